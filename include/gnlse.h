@@ -1,0 +1,163 @@
+/*
+ * gnlse.h -- C ABI of the GB300 GNLSE propagation engine (libgnlse.so).
+ *
+ * The engine replaces the propagation core of pyofss's Fibre module: the
+ * stepper loop, the RK4IP solver and the linear/nonlinear operators it calls.
+ * A host binding (the Python package pyofsschanged_gb300, or a ctypes/cffi
+ * stub in pyofss itself) builds the operator tables exactly as pyofss does and
+ * hands them over through this interface; the whole propagation of one or many
+ * fields then runs on the GPU.
+ *
+ * Reference interfaces each entry point stands in for (paths inside the pyofss
+ * project):
+ *   gnlse_plan_create   Linearity.__call__ / default_linearity
+ *                       (pyofss/modules/linearity.py:158-186),
+ *                       Nonlinearity.__call__ (pyofss/modules/nonlinearity.py:160-185),
+ *                       Amplifier.set_domain / spectal_filtration_array
+ *                       (pyofss/modules/amplifier.py:110-147),
+ *                       Stepper.__init__ (pyofss/modules/stepper.py:87-145)
+ *   gnlse_propagate     Fibre.__call__ (pyofss/modules/fibre.py:136-148) ->
+ *                       Stepper.__call__ (stepper.py:147-156) ->
+ *                       standard_stepper (stepper.py:164-221) /
+ *                       adaptive_stepper (stepper.py:247-376) ->
+ *                       Solver.rk4ip (pyofss/modules/solver.py:339-354)
+ *   gnlse_get_stats     Storage.step_sizes / fft_total (pyofss/modules/storage.py:160-181)
+ *                       and the stepper exceptions (stepper.py:33-47, 350-354, 376)
+ *   traces              Storage.append (storage.py:183-192): z and A(z) per trace
+ *
+ * Conventions: units as pyofss (t ps, nu THz, omega rad/ps, z km, beta_k
+ * ps^k/km, gamma 1/(W km), power W, energy nJ).  Fields are complex
+ * (interleaved re, im) in the time domain, natural order (t from -T/2),
+ * complex64 for GNLSE_FP32 plans and complex128 for GNLSE_FP64 plans.
+ * Spectral tables are in FFT order (pyofss fftshift order).
+ *
+ * All device pointers are plain CUDA device pointers; stream arguments are
+ * cudaStream_t values passed as void*.  Every call returns a status code.
+ * A plan is not thread safe; use one plan per host thread.
+ */
+#ifndef GNLSE_H
+#define GNLSE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GNLSE_ABI_VERSION 1
+
+/* status codes (per call and per instance) */
+enum {
+  GNLSE_OK = 0,
+  GNLSE_SMALL_STEP = 1,      /* SmallStepSizeError (stepper.py:350-351) */
+  GNLSE_SUITABLE_STEP = 2,   /* SuitableStepSizeError (stepper.py:353-354) */
+  GNLSE_MAX_STEPS = 3,       /* MaximumStepsAllocatedError (stepper.py:376) */
+  GNLSE_BAD_ARGUMENT = 4,
+  GNLSE_CUDA_ERROR = 5,
+  GNLSE_UNSUPPORTED = 6,
+  GNLSE_OUT_OF_MEMORY = 7,
+  GNLSE_RUNNING = 8          /* instance not finished (attempt budget reached) */
+};
+
+enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1 };
+enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1 };
+
+/* One grid (pyofss Domain) with the fibre operators built on it. */
+typedef struct {
+  int32_t n;                  /* samples: power of two, 256 .. 65536 (FP64: .. 32768) */
+  int32_t cluster;            /* CTAs per field: 0 = automatic, else 1, 2, 4 or 8 */
+  double dt;                  /* Domain.dt, ps */
+  double window_t;            /* Domain.window_t, ps */
+  const double* beta_w;       /* [n] fftshift(sum_k beta_k (w - w0)^k / k!), 1/km */
+  double alpha;               /* linear attenuation, 1/km (0: none) */
+  double gamma;               /* 1/(W km) */
+  const double* ss_w;         /* [n] 1 + omega * s (FFT order); NULL: no self-steepening */
+  double f_R;                 /* Raman fraction */
+  const double* hR_re;        /* [n] Re fft(h_R) * window_t (FFT order); NULL: no Raman */
+  const double* hR_im;        /* [n] Im of the same */
+  const double* nu;           /* [n] absolute frequency, THz (FFT order); diagnostics */
+  int32_t gain_on;            /* saturable gain (Amplifier) on/off */
+  int32_t pad0;
+  double gain_log;            /* ln(10^(small_signal_gain_dB / 10)) */
+  double E_sat;               /* nJ */
+  double gain_length;         /* amplifier length = fibre length, km */
+  const double* gain_profile; /* [n] spectral gain profile (FFT order) */
+} gnlse_grid_desc;
+
+/* One propagation (one field through one fibre). */
+typedef struct {
+  int32_t grid;               /* index into the grid array */
+  int32_t method;             /* GNLSE_RK4IP (fixed step) or GNLSE_ARK4IP (adaptive) */
+  int32_t total_steps;        /* Fibre total_steps */
+  int32_t traces;             /* Fibre traces (>= 1) */
+  int32_t max_traces;         /* trace slots reserved for this instance (0: none) */
+  int32_t pad0;
+  double length;              /* km */
+  double local_error;         /* adaptive tolerance */
+  double h0;                  /* adaptive initial step, km; <= 0: the stepper's rule */
+} gnlse_instance_desc;
+
+typedef struct {
+  double z;                   /* distance reached, km */
+  double h;                   /* next step size, km */
+  double delta_last;          /* last relative local error estimate */
+  double energy_in, energy_out;      /* FP64 Parseval energy, nJ */
+  double photons_in, photons_out;    /* FP64 photon number */
+  int64_t attempts;           /* step attempts (adaptive) / steps (fixed) */
+  int64_t accepted, rejected;
+  int64_t evals;              /* RK4IP evaluations (3 per adaptive attempt) */
+  int64_t steps;              /* accepted steps */
+  int32_t status;             /* GNLSE_OK / error code / GNLSE_RUNNING */
+  int32_t ntraces;            /* traces written */
+  int32_t trace_overflow;     /* 1 if traces were dropped for lack of slots */
+  int32_t finished;           /* 1 once the output field has been written */
+} gnlse_stats;
+
+typedef struct gnlse_plan gnlse_plan;
+
+int gnlse_abi_version(void);
+const char* gnlse_status_string(int status);
+
+/* Build device tables and scratch for n_instances propagations over n_grids
+ * grids.  precision: GNLSE_FP32 (complex64 state, FP64 phase and control) or
+ * GNLSE_FP64 (complex128 throughout). */
+int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids,
+                      int n_instances, const gnlse_instance_desc* instances,
+                      gnlse_plan** plan_out);
+int gnlse_plan_destroy(gnlse_plan* plan);
+
+/* Layout of the caller's buffers: instance i's field occupies complex
+ * elements [field_offset(i), field_offset(i) + n_i); its trace slots occupy
+ * complex elements [trace_offset(i), trace_offset(i) + max_traces_i * n_i)
+ * and its trace z values doubles [trace_z_offset(i), + max_traces_i). */
+int64_t gnlse_plan_field_elems(const gnlse_plan* plan);
+int64_t gnlse_plan_field_offset(const gnlse_plan* plan, int instance);
+int64_t gnlse_plan_trace_elems(const gnlse_plan* plan);
+int64_t gnlse_plan_trace_offset(const gnlse_plan* plan, int instance);
+int64_t gnlse_plan_trace_z_elems(const gnlse_plan* plan);
+int64_t gnlse_plan_trace_z_offset(const gnlse_plan* plan, int instance);
+int64_t gnlse_plan_scratch_bytes(const gnlse_plan* plan);
+
+/* Mark every instance as not started (the next propagate starts from the
+ * fields it is given). */
+int gnlse_reset(gnlse_plan* plan, void* stream);
+
+/* Propagate all instances, in place on d_fields (device, time domain).
+ * max_attempts > 0 bounds the attempts each instance may spend in this call;
+ * unfinished instances report GNLSE_RUNNING and continue on the next call
+ * (checkpoint / resume between calls).  Asynchronous on `stream`. */
+int gnlse_propagate(gnlse_plan* plan, void* d_fields, void* d_traces, double* d_trace_z,
+                    int64_t max_attempts, void* stream);
+
+/* Same, from and to host memory: copies the fields in, propagates to the end
+ * and copies the fields out (synchronous).  h_in and h_out may alias. */
+int gnlse_propagate_host(gnlse_plan* plan, const void* h_in, void* h_out, void* stream);
+
+/* Copy per-instance statistics to host memory (synchronises `stream`). */
+int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GNLSE_H */

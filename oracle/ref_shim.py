@@ -1,0 +1,155 @@
+"""Load the unmodified pyofss reference (pure Python) in a modern environment.
+
+TEST INFRASTRUCTURE ONLY.  This module is used by ``tests/golden/make_golden.py``
+and by the CPU tests that pin the oracle against the reference itself.  It is
+never imported by the product package, by ``bench.py`` or on the GPU host
+(the reference tree is not present there).
+
+The reference targets an older numpy/scipy stack.  Without touching any file of
+the reference, this shim:
+
+* aliases the scipy names that newer scipy removed (``scipy.power``,
+  ``scipy.log10``, ``scipy.exp``, ``scipy.sqrt``, ``scipy.log``,
+  ``scipy.integrate.simps``) and ``collections.Iterable``;
+* registers empty stand-ins for optional modules the reference imports at
+  module level but never uses on the CPU propagation path (pandas, matplotlib,
+  pyopencl, reikna, pynvml, unittest2);
+* pre-registers ``pyofss`` as a package object with ``__path__`` so that
+  ``pyofss/__init__.py`` (which pulls in the plotter and OpenCL modules) is not
+  executed.
+
+Runtime quirks of the reference that callers must work around:
+
+* ``Stepper.adaptive_stepper`` reads ``storage.dir_spec`` at its end
+  (pyofss/modules/stepper.py:365), an attribute ``Storage`` never defines;
+  :func:`make_fibre` sets ``dir_spec = dir_temp = None`` on the instance.
+* ``Stepper.__call__`` requires ``refrence_length`` (stepper.py:147);
+  ``Fibre.__call__`` supplies it.
+"""
+
+import collections
+import collections.abc
+import importlib
+import os
+import sys
+import types
+
+import numpy as np
+
+REFERENCE_ROOT = os.environ.get("PYOFSS_REFERENCE", "/root/reference")
+
+
+class _Stub(types.ModuleType):
+    """Module stand-in: any attribute is another stub (callable, subclassable)."""
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        sub = _Stub(f"{self.__name__}.{name}")
+        setattr(self, name, sub)
+        return sub
+
+    def __call__(self, *args, **kwargs):
+        return _Stub(self.__name__ + "()")
+
+    def __mro_entries__(self, bases):
+        return (object,)
+
+
+def available():
+    return os.path.isdir(os.path.join(REFERENCE_ROOT, "pyofss"))
+
+
+_loaded = None
+
+
+def load():
+    """Import the reference's CPU propagation modules; return a namespace."""
+    global _loaded
+    if _loaded is not None:
+        return _loaded
+    if not available():
+        raise RuntimeError(f"pyofss reference tree not found at {REFERENCE_ROOT}")
+    sys.dont_write_bytecode = True
+
+    import scipy
+    import scipy.integrate
+
+    for name in ("power", "log10", "exp", "sqrt", "log"):
+        if not hasattr(scipy, name):
+            setattr(scipy, name, getattr(np, name))
+    if not hasattr(scipy.integrate, "simps"):
+        scipy.integrate.simps = scipy.integrate.simpson
+    if not hasattr(collections, "Iterable"):
+        collections.Iterable = collections.abc.Iterable
+
+    for mod in ("pandas", "matplotlib", "matplotlib.pyplot", "pyopencl",
+                "pyopencl.array", "reikna", "reikna.cluda", "reikna.fft",
+                "pynvml", "unittest2", "tqdm"):
+        if mod not in sys.modules:
+            try:
+                importlib.import_module(mod)
+            except Exception:
+                sys.modules[mod] = _Stub(mod)
+
+    if "pyofss" not in sys.modules:
+        pkg = types.ModuleType("pyofss")
+        pkg.__path__ = [os.path.join(REFERENCE_ROOT, "pyofss")]
+        sys.modules["pyofss"] = pkg
+        mods = types.ModuleType("pyofss.modules")
+        mods.__path__ = [os.path.join(REFERENCE_ROOT, "pyofss", "modules")]
+        sys.modules["pyofss.modules"] = mods
+
+    ns = types.SimpleNamespace()
+    ns.field = importlib.import_module("pyofss.field")
+    ns.domain = importlib.import_module("pyofss.domain")
+    ns.solver = importlib.import_module("pyofss.modules.solver")
+    ns.stepper = importlib.import_module("pyofss.modules.stepper")
+    ns.linearity = importlib.import_module("pyofss.modules.linearity")
+    ns.nonlinearity = importlib.import_module("pyofss.modules.nonlinearity")
+    ns.amplifier = importlib.import_module("pyofss.modules.amplifier")
+    ns.fibre = importlib.import_module("pyofss.modules.fibre")
+    ns.sech = importlib.import_module("pyofss.modules.sech")
+    ns.gaussian = importlib.import_module("pyofss.modules.gaussian")
+    ns.Domain = ns.domain.Domain
+    ns.Fibre = ns.fibre.Fibre
+    ns.Sech = ns.sech.Sech
+    ns.Gaussian = ns.gaussian.Gaussian
+    ns.Stepper = ns.stepper.Stepper
+    _loaded = ns
+    return ns
+
+
+def make_fibre(**kwargs):
+    """Build a reference ``Fibre`` with the adaptive-stepper end-of-run quirk patched."""
+    ref = load()
+    fib = ref.Fibre(**kwargs)
+    fib.stepper.storage.dir_spec = None
+    fib.stepper.storage.dir_temp = None
+    # Storage.update_characts calls scipy find_peaks per trace; harmless, but
+    # the characteristic lists are host analysis outside the propagation path.
+    return fib
+
+
+class StepLog:
+    """Record every ``Solver.rk4ip`` call (z, h) made by a reference run."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __enter__(self):
+        ref = load()
+        self._orig = ref.solver.Solver.rk4ip
+        log = self.calls
+        orig = self._orig
+
+        def logged(A, z, h, f):
+            log.append((float(z), float(h)))
+            return orig(A, z, h, f)
+
+        ref.solver.Solver.rk4ip = staticmethod(logged)
+        return self
+
+    def __exit__(self, *exc):
+        load().solver.Solver.rk4ip = staticmethod(self._orig)
+        return False

@@ -1,0 +1,455 @@
+// C-ABI of the GNLSE engine: plan construction (device operator tables in the
+// cluster-permuted layout), class dispatch and propagation driver.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/gnlse.h"
+#include "gnlse_launch.h"
+#include "gnlse_types.h"
+
+using namespace gnlse;
+
+namespace {
+
+struct ClassRun {
+  int logm, C;
+  int first;  // offset into the order array
+  int count;
+};
+
+struct GridHost {
+  int n, logm, C;
+  void* d_beta = nullptr;
+  void* d_Kr = nullptr;
+  void* d_Hp = nullptr;
+  void* d_lor = nullptr;
+  void* d_nu = nullptr;
+  void* d_tw = nullptr;
+};
+
+bool supported(int precision, int logm, int C) {
+#define GNLSE_MATCH(R, L, CC) \
+  if ((sizeof(R) == 8) == (precision == GNLSE_FP64) && logm == (L) && C == (CC)) return true;
+  GNLSE_CLASSES_F32(GNLSE_MATCH)
+  GNLSE_CLASSES_F64(GNLSE_MATCH)
+#undef GNLSE_MATCH
+  return false;
+}
+
+cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, cudaStream_t s) {
+#define GNLSE_CALL(R, L, CC)                                                     \
+  if ((sizeof(R) == 8) == (precision == GNLSE_FP64) && logm == (L) && C == (CC)) \
+    return launch_class<R, L, CC>(kp, n, s);
+  GNLSE_CLASSES_F32(GNLSE_CALL)
+  GNLSE_CLASSES_F64(GNLSE_CALL)
+#undef GNLSE_CALL
+  return cudaErrorInvalidValue;
+}
+
+int ilog2i(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+}  // namespace
+
+struct gnlse_plan {
+  int precision = 0;
+  size_t vsize = 8;
+  int device = 0;
+  std::vector<GridHost> grids;
+  std::vector<InstDev> inst;
+  std::vector<int> order;
+  std::vector<ClassRun> classes;
+  GridDev* d_grids = nullptr;
+  InstDev* d_inst = nullptr;
+  InstState* d_state = nullptr;
+  int* d_order = nullptr;
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  int64_t field_elems = 0, trace_elems = 0, tracez_elems = 0;
+  std::vector<int64_t> field_off, trace_off, tracez_off;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> ev;
+  cudaEvent_t fork = nullptr;
+  // host-buffer entry point staging
+  void* d_io = nullptr;
+  void* d_tr = nullptr;
+  double* d_trz = nullptr;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e) {
+  if (e == cudaErrorMemoryAllocation) return GNLSE_OUT_OF_MEMORY;
+  return GNLSE_CUDA_ERROR;
+}
+
+template <class T>
+cudaError_t upload(gnlse_plan* p, const std::vector<T>& h, void** d) {
+  cudaError_t e = cudaMalloc(d, h.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  p->allocs.push_back(*d);
+  return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+template <class R>
+cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost& gh, GridDev& dv) {
+  const int n = gd.n, C = gh.C, M = n / C;
+  auto perm = [&](int a) { return (a % M) * C + a / M; };  // slot a = c*M + k2  <-  k = c + C*k2
+  std::vector<double> beta(n), nu(n);
+  std::vector<R> Kr(n), lor, Hp;
+  std::vector<R> tw(2 * (size_t)n);
+  for (int a = 0; a < n; ++a) {
+    const int k = perm(a);
+    beta[a] = gd.beta_w[k];
+    nu[a] = gd.nu ? gd.nu[k] : 1.0;
+    Kr[a] = (R)(gd.gamma * (gd.ss_w ? gd.ss_w[k] : 1.0));
+  }
+  const bool raman = gd.hR_re != nullptr;
+  if (raman) {
+    Hp.resize(2 * (size_t)n);
+    for (int a = 0; a < n; ++a) {
+      const int k = perm(a);
+      Hp[2 * a] = (R)(gd.hR_re[k] / n);
+      Hp[2 * a + 1] = (R)((gd.hR_im ? gd.hR_im[k] : 0.0) / n);
+    }
+  }
+  if (gd.gain_on) {
+    lor.resize(n);
+    for (int a = 0; a < n; ++a) lor[a] = (R)(gd.gain_profile ? gd.gain_profile[perm(a)] : 1.0);
+  }
+  // exp(+2 pi i j / n): reduce j to the first octant for an accurate argument
+  for (int j = 0; j < n; ++j) {
+    const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)j / (long double)n;
+    tw[2 * (size_t)j] = (R)std::cos((double)ang);
+    tw[2 * (size_t)j + 1] = (R)std::sin((double)ang);
+  }
+  cudaError_t e;
+  if ((e = upload(p, beta, &gh.d_beta)) != cudaSuccess) return e;
+  if ((e = upload(p, nu, &gh.d_nu)) != cudaSuccess) return e;
+  if ((e = upload(p, Kr, &gh.d_Kr)) != cudaSuccess) return e;
+  if ((e = upload(p, tw, &gh.d_tw)) != cudaSuccess) return e;
+  if (raman && (e = upload(p, Hp, &gh.d_Hp)) != cudaSuccess) return e;
+  if (gd.gain_on && (e = upload(p, lor, &gh.d_lor)) != cudaSuccess) return e;
+  dv.beta = (const double*)gh.d_beta;
+  dv.Kr = gh.d_Kr;
+  dv.Hp = raman ? gh.d_Hp : nullptr;
+  dv.lor = gd.gain_on ? gh.d_lor : nullptr;
+  dv.nu = (const double*)gh.d_nu;
+  dv.tw = gh.d_tw;
+  dv.n = n;
+  dv.logm = gh.logm;
+  dv.C = C;
+  dv.raman = raman ? 1 : 0;
+  dv.gain = gd.gain_on ? 1 : 0;
+  dv.alpha = gd.alpha;
+  dv.fR = gd.f_R;
+  dv.gain_log = gd.gain_log;
+  dv.E_sat = gd.E_sat;
+  dv.gain_len = gd.gain_length;
+  dv.dt = gd.dt;
+  dv.window_t = gd.window_t;
+  return cudaSuccess;
+}
+
+void free_plan(gnlse_plan* p) {
+  for (void* a : p->allocs) cudaFree(a);
+  for (auto s : p->side) cudaStreamDestroy(s);
+  for (auto e : p->ev) cudaEventDestroy(e);
+  if (p->fork) cudaEventDestroy(p->fork);
+  delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gnlse_abi_version(void) { return GNLSE_ABI_VERSION; }
+
+const char* gnlse_status_string(int s) {
+  switch (s) {
+    case GNLSE_OK: return "ok";
+    case GNLSE_SMALL_STEP: return "Step size is extremely small";
+    case GNLSE_SUITABLE_STEP: return "Failed to set suitable step-size";
+    case GNLSE_MAX_STEPS: return "Failed to complete with maximum steps allocated";
+    case GNLSE_BAD_ARGUMENT: return "bad argument";
+    case GNLSE_CUDA_ERROR: return "CUDA error";
+    case GNLSE_UNSUPPORTED: return "unsupported grid size / precision / cluster size";
+    case GNLSE_OUT_OF_MEMORY: return "out of device memory";
+    case GNLSE_RUNNING: return "running (attempt budget reached)";
+    default: return "unknown status";
+  }
+}
+
+int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, int n_instances,
+                      const gnlse_instance_desc* instances, gnlse_plan** plan_out) {
+  if (!plan_out || !grids || !instances || n_grids <= 0 || n_instances <= 0) return GNLSE_BAD_ARGUMENT;
+  if (precision != GNLSE_FP32 && precision != GNLSE_FP64) return GNLSE_BAD_ARGUMENT;
+  *plan_out = nullptr;
+  gnlse_plan* p = new (std::nothrow) gnlse_plan();
+  if (!p) return GNLSE_OUT_OF_MEMORY;
+  p->precision = precision;
+  p->vsize = precision == GNLSE_FP64 ? 16 : 8;
+  cudaGetDevice(&p->device);
+  std::vector<GridDev> gdev(n_grids);
+  p->grids.resize(n_grids);
+  for (int i = 0; i < n_grids; ++i) {
+    const gnlse_grid_desc& gd = grids[i];
+    const int n = gd.n;
+    if (n < 256 || (n & (n - 1)) != 0 || !gd.beta_w || !(gd.dt > 0) || !(gd.window_t > 0) ||
+        (gd.gain_on && !(gd.E_sat > 0 && gd.gain_length > 0))) {
+      free_plan(p);
+      return GNLSE_BAD_ARGUMENT;
+    }
+    int C = gd.cluster;
+    const int mmax = precision == GNLSE_FP64 ? 4096 : 8192;
+    if (C == 0) C = n <= mmax ? 1 : n / mmax;
+    if (C != 1 && C != 2 && C != 4 && C != 8) {
+      free_plan(p);
+      return GNLSE_UNSUPPORTED;
+    }
+    const int logm = ilog2i(n / C);
+    if (n % C != 0 || !supported(precision, logm, C)) {
+      free_plan(p);
+      return GNLSE_UNSUPPORTED;
+    }
+    GridHost& gh = p->grids[i];
+    gh.n = n;
+    gh.logm = logm;
+    gh.C = C;
+    cudaError_t e = precision == GNLSE_FP64 ? build_grid_tables<double>(p, gd, gh, gdev[i])
+                                            : build_grid_tables<float>(p, gd, gh, gdev[i]);
+    if (e != cudaSuccess) {
+      free_plan(p);
+      return cuda_fail(e);
+    }
+  }
+  p->inst.resize(n_instances);
+  p->field_off.resize(n_instances);
+  p->trace_off.resize(n_instances);
+  p->tracez_off.resize(n_instances);
+  int64_t foff = 0, soff = 0, toff = 0, zoff = 0;
+  for (int i = 0; i < n_instances; ++i) {
+    const gnlse_instance_desc& id = instances[i];
+    if (id.grid < 0 || id.grid >= n_grids || (id.method != GNLSE_RK4IP && id.method != GNLSE_ARK4IP) ||
+        id.total_steps < 1 || id.traces < 1 || id.max_traces < 0 || !(id.length >= 0) ||
+        (id.method == GNLSE_ARK4IP && !(id.local_error > 0))) {
+      free_plan(p);
+      return GNLSE_BAD_ARGUMENT;
+    }
+    const int n = p->grids[id.grid].n;
+    InstDev& d = p->inst[i];
+    memset(&d, 0, sizeof(d));
+    d.grid = id.grid;
+    d.method = id.method;
+    d.total_steps = id.total_steps;
+    d.traces = id.traces;
+    d.max_traces = id.max_traces;
+    d.length = id.length;
+    d.tol = id.local_error;
+    double h0 = id.h0;
+    if (!(h0 > 0)) {  // stepper.py:256-264
+      h0 = id.traces > id.total_steps ? id.length / id.traces : id.length / id.total_steps;
+      if (h0 > 1e-6) h0 = 1e-6;
+    }
+    d.h0 = h0;
+    d.field_off = foff;
+    d.scratch_off = soff;
+    d.trace_off = toff;
+    d.tracez_off = zoff;
+    p->field_off[i] = foff;
+    p->trace_off[i] = toff;
+    p->tracez_off[i] = zoff;
+    foff += n;
+    soff += 8 * (int64_t)n;
+    toff += (int64_t)id.max_traces * n;
+    zoff += id.max_traces;
+  }
+  p->field_elems = foff;
+  p->trace_elems = toff;
+  p->tracez_elems = zoff;
+  p->scratch_bytes = (size_t)soff * p->vsize;
+  // classes: instances grouped by (logm, C), longest estimated work first
+  std::vector<int> ids(n_instances);
+  for (int i = 0; i < n_instances; ++i) ids[i] = i;
+  auto cls = [&](int i) { const GridHost& g = p->grids[p->inst[i].grid]; return g.logm * 16 + g.C; };
+  auto cost = [&](int i) {
+    const GridHost& g = p->grids[p->inst[i].grid];
+    return p->inst[i].length * (double)g.n * std::log2((double)g.n);
+  };
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) {
+    if (cls(a) != cls(b)) return cls(a) < cls(b);
+    return cost(a) > cost(b);
+  });
+  p->order = ids;
+  for (int k = 0; k < n_instances;) {
+    int j = k;
+    while (j < n_instances && cls(ids[j]) == cls(ids[k])) ++j;
+    const GridHost& g = p->grids[p->inst[ids[k]].grid];
+    p->classes.push_back({g.logm, g.C, k, j - k});
+    k = j;
+  }
+  cudaError_t e;
+  void* ptr = nullptr;
+  if ((e = upload(p, gdev, &ptr)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  p->d_grids = (GridDev*)ptr;
+  if ((e = upload(p, p->inst, &ptr)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  p->d_inst = (InstDev*)ptr;
+  if ((e = upload(p, p->order, &ptr)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  p->d_order = (int*)ptr;
+  if ((e = cudaMalloc(&ptr, sizeof(InstState) * n_instances)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  p->allocs.push_back(ptr);
+  p->d_state = (InstState*)ptr;
+  cudaMemset(p->d_state, 0, sizeof(InstState) * n_instances);
+  if ((e = cudaMalloc(&p->d_scratch, p->scratch_bytes)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  p->allocs.push_back(p->d_scratch);
+  for (size_t c = 0; c < p->classes.size(); ++c) {
+    cudaStream_t s;
+    cudaEvent_t ev;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      free_plan(p);
+      return GNLSE_CUDA_ERROR;
+    }
+    p->side.push_back(s);
+    p->ev.push_back(ev);
+  }
+  if (cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) != cudaSuccess) {
+    free_plan(p);
+    return GNLSE_CUDA_ERROR;
+  }
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
+  *plan_out = p;
+  return GNLSE_OK;
+}
+
+int gnlse_plan_destroy(gnlse_plan* p) {
+  if (!p) return GNLSE_BAD_ARGUMENT;
+  cudaDeviceSynchronize();
+  free_plan(p);
+  return GNLSE_OK;
+}
+
+int64_t gnlse_plan_field_elems(const gnlse_plan* p) { return p ? p->field_elems : -1; }
+int64_t gnlse_plan_field_offset(const gnlse_plan* p, int i) {
+  return (p && i >= 0 && i < (int)p->inst.size()) ? p->field_off[i] : -1;
+}
+int64_t gnlse_plan_trace_elems(const gnlse_plan* p) { return p ? p->trace_elems : -1; }
+int64_t gnlse_plan_trace_offset(const gnlse_plan* p, int i) {
+  return (p && i >= 0 && i < (int)p->inst.size()) ? p->trace_off[i] : -1;
+}
+int64_t gnlse_plan_trace_z_elems(const gnlse_plan* p) { return p ? p->tracez_elems : -1; }
+int64_t gnlse_plan_trace_z_offset(const gnlse_plan* p, int i) {
+  return (p && i >= 0 && i < (int)p->inst.size()) ? p->tracez_off[i] : -1;
+}
+int64_t gnlse_plan_scratch_bytes(const gnlse_plan* p) { return p ? (int64_t)p->scratch_bytes : -1; }
+
+int gnlse_reset(gnlse_plan* p, void* stream) {
+  if (!p) return GNLSE_BAD_ARGUMENT;
+  cudaError_t e = cudaMemsetAsync(p->d_state, 0, sizeof(InstState) * p->inst.size(), (cudaStream_t)stream);
+  return e == cudaSuccess ? GNLSE_OK : cuda_fail(e);
+}
+
+int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_trace_z,
+                    int64_t max_attempts, void* stream) {
+  if (!p || !d_fields) return GNLSE_BAD_ARGUMENT;
+  if (p->trace_elems > 0 && (!d_traces || !d_trace_z)) return GNLSE_BAD_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  KParams kp = {};
+  kp.inst = p->d_inst;
+  kp.state = p->d_state;
+  kp.grids = p->d_grids;
+  kp.fields = d_fields;
+  kp.scratch = p->d_scratch;
+  kp.traces = d_traces;
+  kp.trace_z = d_trace_z;
+  kp.max_attempts = max_attempts;
+  cudaError_t e;
+  if (p->classes.size() == 1) {
+    const ClassRun& c = p->classes[0];
+    kp.order = p->d_order + c.first;
+    kp.n_order = c.count;
+    e = dispatch(p->precision, c.logm, c.C, kp, c.count, s);
+    return e == cudaSuccess ? GNLSE_OK : cuda_fail(e);
+  }
+  // several classes: fork onto side streams so they share the GPU, then join
+  if ((e = cudaEventRecord(p->fork, s)) != cudaSuccess) return cuda_fail(e);
+  for (size_t k = 0; k < p->classes.size(); ++k) {
+    const ClassRun& c = p->classes[k];
+    if ((e = cudaStreamWaitEvent(p->side[k], p->fork, 0)) != cudaSuccess) return cuda_fail(e);
+    kp.order = p->d_order + c.first;
+    kp.n_order = c.count;
+    if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if ((e = cudaEventRecord(p->ev[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if ((e = cudaStreamWaitEvent(s, p->ev[k], 0)) != cudaSuccess) return cuda_fail(e);
+  }
+  return GNLSE_OK;
+}
+
+int gnlse_propagate_host(gnlse_plan* p, const void* h_in, void* h_out, void* stream) {
+  if (!p || !h_in || !h_out) return GNLSE_BAD_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = (size_t)p->field_elems * p->vsize;
+  cudaError_t e;
+  if (!p->d_io) {
+    if ((e = cudaMalloc(&p->d_io, bytes)) != cudaSuccess) return cuda_fail(e);
+    p->allocs.push_back(p->d_io);
+    if (p->trace_elems > 0) {
+      if ((e = cudaMalloc(&p->d_tr, (size_t)p->trace_elems * p->vsize)) != cudaSuccess) return cuda_fail(e);
+      p->allocs.push_back(p->d_tr);
+      if ((e = cudaMalloc((void**)&p->d_trz, sizeof(double) * p->tracez_elems)) != cudaSuccess) return cuda_fail(e);
+      p->allocs.push_back(p->d_trz);
+    }
+  }
+  if ((e = cudaMemcpyAsync(p->d_io, h_in, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) return cuda_fail(e);
+  int rc = gnlse_reset(p, stream);
+  if (rc != GNLSE_OK) return rc;
+  rc = gnlse_propagate(p, p->d_io, p->d_tr, p->d_trz, 0, stream);
+  if (rc != GNLSE_OK) return rc;
+  if ((e = cudaMemcpyAsync(h_out, p->d_io, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_fail(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
+  return GNLSE_OK;
+}
+
+int gnlse_get_stats(gnlse_plan* p, gnlse_stats* out, void* stream) {
+  if (!p || !out) return GNLSE_BAD_ARGUMENT;
+  const size_t n = p->inst.size();
+  std::vector<InstState> st(n);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(st.data(), p->d_state, sizeof(InstState) * n, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
+  for (size_t i = 0; i < n; ++i) {
+    gnlse_stats& o = out[i];
+    const InstState& t = st[i];
+    o.z = t.z;
+    o.h = t.h;
+    o.delta_last = t.delta_last;
+    o.energy_in = t.E_in;
+    o.energy_out = t.E_out;
+    o.photons_in = t.Nph_in;
+    o.photons_out = t.Nph_out;
+    o.attempts = t.attempts;
+    o.accepted = t.accepted;
+    o.rejected = t.rejected;
+    o.evals = t.evals;
+    o.steps = t.steps;
+    o.status = t.phase == 0 ? GNLSE_RUNNING : (t.phase == 3 ? t.status : GNLSE_RUNNING);
+    if (t.phase == 3 || t.phase == 2) o.status = t.status;
+    o.ntraces = t.ntraces;
+    o.trace_overflow = t.trace_overflow;
+    o.finished = t.phase == 3 ? 1 : 0;
+  }
+  return GNLSE_OK;
+}
+
+}  // extern "C"

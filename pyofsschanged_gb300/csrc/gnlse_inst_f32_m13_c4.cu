@@ -1,0 +1,3 @@
+// Kernel instantiation: float, M = 2^13 points per CTA, cluster of 4.
+#include "gnlse_inst.inc"
+GNLSE_INSTANTIATE(float, 13, 4)

@@ -1,0 +1,3 @@
+// Kernel instantiation: double, M = 2^8 points per CTA, cluster of 2.
+#include "gnlse_inst.inc"
+GNLSE_INSTANTIATE(double, 8, 2)

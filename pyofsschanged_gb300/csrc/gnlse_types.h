@@ -1,0 +1,74 @@
+// Shared host/device descriptors of the GNLSE engine.  Plain C structs: they
+// cross the boundary between the C-ABI layer and the kernels only, never the
+// public ABI (include/gnlse.h), which has its own descriptor types.
+#pragma once
+#include <stdint.h>
+
+namespace gnlse {
+
+// Per grid (one Domain + one set of fibre operators).  All spectral tables are
+// stored in the cluster-permuted layout: entry a = c*M + k2 holds frequency
+// index k = c + C*k2 (FFT order), where C is the cluster size and M = N/C.
+struct GridDev {
+  const double* beta;   // [N] sum_n beta_n (w-w0)^n/n!   (1/km), FP64
+  const void* Kr;       // [N] real: gamma * (1 + omega * s)
+  const void* Hp;       // [N] complex: fft(h_R) * window_t / N   (null: no Raman)
+  const void* lor;      // [N] real: gain profile                   (null: no gain)
+  const double* nu;     // [N] absolute frequency (THz), FP64, for photon number
+  const void* tw;       // [N] natural order: exp(+2 pi i j / N)
+  int n, logm, C, raman;
+  int gain, pad0;
+  double alpha;         // 1/km, linear attenuation
+  double fR;            // Raman fraction
+  double gain_log;      // ln(10^(gain_dB/10))
+  double E_sat;         // nJ
+  double gain_len;      // km (amplifier length = fibre length)
+  double dt;            // ps
+  double window_t;      // ps
+};
+
+struct InstDev {
+  int grid;             // index into GridDev array
+  int method;           // 0: fixed-step RK4IP, 1: adaptive (ARK4IP)
+  int total_steps;      // fixed-step count / adaptive initial-step rule
+  int traces;           // pyofss 'traces' argument
+  int max_traces;       // capacity of this instance's trace slots
+  int pad0;
+  double length;        // km
+  double tol;           // local error (adaptive)
+  double h0;            // initial step (adaptive), km
+  long long field_off;  // element offset of the time-domain field (in/out)
+  long long scratch_off;// element offset of the 8*N scratch block
+  long long trace_off;  // element offset of max_traces*N trace slots
+  long long tracez_off; // index of this instance's first trace z value
+};
+
+enum : int {
+  ST_OK = 0, ST_SMALL_STEP = 1, ST_SUITABLE_STEP = 2, ST_MAX_STEPS = 3,
+  ST_BAD_ARG = 4, ST_RUNNING = 8
+};
+
+struct InstState {
+  double z, h, z_ignore, delta_last;
+  double E_in, E_out, Nph_in, Nph_out;
+  double cache_eA, cache_eN;  // gain energies of the cached state
+  long long attempts, accepted, rejected, evals, steps, ffts;
+  int status, ntraces, phase, sidx;
+  int ma_valid, ta, trace_overflow, pad0;
+};
+
+struct KParams {
+  const InstDev* inst;
+  InstState* state;
+  const int* order;     // instance ids handled by this launch (one per cluster)
+  int n_order;
+  int pad0;
+  const GridDev* grids;
+  void* fields;         // base of time-domain fields (complex R)
+  void* scratch;        // base of scratch (complex R)
+  void* traces;         // base of trace slots (complex R)
+  double* trace_z;      // trace z values, instance slots start at InstDev::tracez_off
+  long long max_attempts;  // attempts this launch may spend per instance (<=0: unbounded)
+};
+
+}  // namespace gnlse

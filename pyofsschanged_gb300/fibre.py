@@ -1,0 +1,159 @@
+"""``Fibre`` module with CUDA RK4IP / ARK4IP methods (drop-in for pyofss's Fibre).
+
+Constructor arguments are those of ``pyofss.modules.fibre.Fibre``
+(pyofss/modules/fibre.py:74-134); calling the module with ``(domain, field)``
+propagates the field through the fibre and returns it, as
+``Fibre.__call__`` does (fibre.py:136-148).  ``method`` selects the engine
+path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps) or
+``"cuda_ark4ip"`` / ``"ark4ip"`` (adaptive step doubling with tolerance
+``local_error``).  ``precision`` selects complex64 (``"fp32"``, default) or
+complex128 (``"fp64"``) propagation.  The stepper exceptions of
+pyofss/modules/stepper.py:33-47 are raised with the same names.
+
+Models outside the CUDA path (WDM two-channel, the legacy ``raman_scattering``
+rs_factor terms, Er/Yb gain models, ASE noise) raise ``NotImplementedError``.
+"""
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .engine import Instance, Plan
+from .operators import GridTables
+
+
+class StepperError(Exception):
+    pass
+
+
+class SmallStepSizeError(StepperError):
+    pass
+
+
+class SuitableStepSizeError(StepperError):
+    pass
+
+
+class MaximumStepsAllocatedError(StepperError):
+    pass
+
+
+_STATUS_EXC = {
+    nat.GNLSE_SMALL_STEP: (SmallStepSizeError, "Step size is extremely small"),
+    nat.GNLSE_SUITABLE_STEP: (SuitableStepSizeError, "Failed to set suitable step-size"),
+    nat.GNLSE_MAX_STEPS: (MaximumStepsAllocatedError,
+                          "Failed to complete with maximum steps allocated"),
+}
+
+
+def raise_for_status(status):
+    if status in _STATUS_EXC:
+        cls, msg = _STATUS_EXC[status]
+        raise cls(msg)
+    if status != nat.GNLSE_OK:
+        raise nat.GnlseError(status, "propagation")
+
+
+class Storage:
+    """Trace store with the fields pyofss's Storage exposes (storage.py:140-192)."""
+
+    def __init__(self):
+        self.z = []
+        self.As = []
+        self.step_sizes = []
+        self.fft_total = 0
+        self.domain = None
+
+    def __call__(self, domain):
+        self.domain = domain
+
+    def reset_array(self):
+        self.z, self.As = [], []
+
+
+class _StepperView:
+    def __init__(self, method, traces, local_error, total_steps, length):
+        self.method = method
+        self.adaptive = method == "ark4ip"
+        self.traces = traces
+        self.local_error = local_error
+        self.total_steps = total_steps
+        self.length = length
+        self.storage = Storage()
+        self.stats = None
+
+
+class Fibre:
+    def __init__(self, name="fibre", length=1.0, alpha=None, beta=None, gamma=0.0, sim_type=None,
+                 traces=1, local_error=1.0e-6, method="cuda_ark4ip", total_steps=100,
+                 self_steepening=False, raman_scattering=False, rs_factor=0.003, use_all=False,
+                 centre_omega=None, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18,
+                 small_signal_gain=None, E_sat=None, P_sat=None, Tr=None, lamb0=None,
+                 bandwidth=None, use_Er_profile=False, use_Er_noise=False, use_Yb_model=False,
+                 Pp_0=None, N=None, Rr=None, dir=None, save_represent="power", cycle=None,
+                 downsampling=None, precision="fp32", cluster=0):
+        m = method.lower()
+        if m.startswith("cuda_"):
+            m = m[5:]
+        if m not in ("rk4ip", "ark4ip"):
+            raise NotImplementedError(f"method {method!r}: the CUDA engine runs rk4ip / ark4ip")
+        if sim_type not in (None, "default"):
+            raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
+        if raman_scattering and not use_all:
+            raise NotImplementedError("legacy rs_factor Raman model is not on the CUDA path")
+        if use_Er_profile or use_Er_noise or use_Yb_model:
+            raise NotImplementedError("Er/Yb gain models and ASE noise are not on the CUDA path")
+        if small_signal_gain is not None and E_sat is None and P_sat is not None:
+            if Tr is None:
+                raise Exception("Repetition rate is not defined.")
+            E_sat = P_sat * Tr
+        self.name = name
+        self.length = length
+        self.alpha, self.beta, self.gamma = alpha, beta, gamma
+        self.self_steepening, self.use_all = self_steepening, use_all
+        self.tau_1, self.tau_2, self.f_R = tau_1, tau_2, f_R
+        self.centre_omega = centre_omega
+        self.small_signal_gain, self.E_sat = small_signal_gain, E_sat
+        self.lamb0, self.bandwidth = lamb0, bandwidth
+        self.method = m
+        self.precision = precision
+        self.cluster = cluster
+        self.cycle = cycle
+        self.domain = None
+        self._plan = None
+        self.stepper = _StepperView(m, traces, local_error, total_steps, length)
+
+    def _build(self, domain):
+        g = GridTables(domain, beta=self.beta, alpha=self.alpha, gamma=self.gamma,
+                       self_steepening=self.self_steepening, use_all=self.use_all,
+                       tau_1=self.tau_1, tau_2=self.tau_2, f_R=self.f_R,
+                       centre_omega=self.centre_omega, small_signal_gain=self.small_signal_gain,
+                       E_sat=self.E_sat, length=self.length, lamb0=self.lamb0,
+                       bandwidth=self.bandwidth, cluster=self.cluster)
+        st = self.stepper
+        inst = Instance(0, method=st.method, length=self.length, local_error=st.local_error,
+                        total_steps=st.total_steps, traces=st.traces)
+        self._plan = Plan([g], [inst], precision=self.precision)
+        self.domain = domain
+        st.storage(domain)
+
+    def __call__(self, domain, field):
+        if self.domain != domain or self._plan is None:
+            self._build(domain)
+        plan = self._plan
+        flat = plan.pack([np.asarray(field)])
+        plan.propagate(flat)
+        stats = plan.stats()
+        torch.cuda.current_stream(plan.device).synchronize()
+        st = stats[0]
+        self.stepper.stats = st
+        storage = self.stepper.storage
+        storage.reset_array()
+        z, As = plan.instance_traces(0, stats)
+        storage.z = list(z)
+        storage.As = [a.astype(complex) for a in As]
+        if self.stepper.adaptive:
+            storage.step_sizes = []
+        storage.fft_total = int(st["evals"]) * 16
+        raise_for_status(st["status"])
+        return plan.unpack(flat)[0].cpu().numpy().astype(complex)

@@ -1,0 +1,41 @@
+"""Load the golden fixtures made by tests/golden/make_golden.py."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    case = {k: z[k] for k in z.files if k != "params"}
+    case["params"] = json.loads(str(z["params"]))
+    case["name"] = name
+    return case
+
+
+def domain_kwargs(params):
+    d = dict(params["domain"])
+    if "lambda_nm" in d:
+        lam = d.pop("lambda_nm")
+        d["centre_nu"] = 1.0e-3 * 299792458.0 / lam
+    return d
+
+
+def fibre_kwargs(params):
+    return dict(params["fibre"])
+
+
+def accepted_steps(calls, adaptive):
+    """(z, h) of the accepted steps from the logged rk4ip calls of a reference run."""
+    if not adaptive:
+        return calls
+    att = calls.reshape(-1, 3, 2)
+    zs, hs = att[:, 0, 0], att[:, 2, 1]
+    acc = [i for i in range(len(zs) - 1) if zs[i + 1] > zs[i]] + [len(zs) - 1]
+    return np.stack([zs[acc], hs[acc]], axis=1)

@@ -1,0 +1,168 @@
+"""Parity of the CUDA engine (through the C ABI) with the reference's golden vectors.
+
+FP64 plans must match the reference output within 1e-9 relative L2 with the
+same number of RK4IP evaluations; FP32 plans must match the reference
+spectrum within 1e-4 relative L2 (the benchmark spec's bound for the complex64 bulk).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import golden_cases as gc
+from oracle import gnlse_oracle as go
+from pyofsschanged_gb300 import Domain, GridTables, Instance, Plan
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-9
+FP32_SPEC_TOL = 1e-4
+FAST = [n for n in gc.names() if n != "sc_cfg_8192"]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def spec_err(a, b):
+    return rel_l2(go.fft(a), go.fft(b))
+
+
+def make_plan(case, precision, cluster=0, max_traces=None):
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    fk = gc.fibre_kwargs(prm)
+    method = fk.pop("method")
+    total_steps = fk.pop("total_steps", 100)
+    traces = fk.pop("traces", 1)
+    tol = fk.pop("local_error", 1e-6)
+    length = fk["length"]
+    g = GridTables(d, cluster=cluster, **fk)
+    inst = Instance(0, method=method, length=length, local_error=tol, total_steps=total_steps,
+                    traces=traces, max_traces=max_traces)
+    return Plan([g], [inst], precision=precision)
+
+
+def run(case, precision, cluster=0):
+    plan = make_plan(case, precision, cluster)
+    f = plan.pack([case["A0"]])
+    plan.propagate(f)
+    st = plan.stats()[0]
+    return plan, plan.unpack(f)[0].cpu().numpy().astype(complex), st
+
+
+@pytest.mark.parametrize("name", FAST)
+def test_fp64_matches_reference(cuda_ready, name):
+    case = gc.load(name)
+    plan, out, st = run(case, "fp64")
+    assert st["status"] == 0 and st["finished"] == 1
+    assert st["evals"] == len(case["rk4ip_calls"])
+    assert rel_l2(out, case["A_out"]) <= FP64_TOL
+    assert spec_err(out, case["A_out"]) <= FP64_TOL
+
+
+@pytest.mark.parametrize("name", FAST)
+def test_fp32_matches_reference(cuda_ready, name):
+    case = gc.load(name)
+    plan, out, st = run(case, "fp32")
+    assert st["status"] == 0 and st["finished"] == 1
+    assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
+    # the step-size controller sees FP32 round-off; the attempt count stays close
+    n_ref = len(case["rk4ip_calls"])
+    assert abs(st["evals"] - n_ref) <= max(3, 0.05 * n_ref)
+
+
+@pytest.mark.parametrize("name,precision,cluster", [
+    ("sc_blowwood_ark4ip_1024", "fp64", 2), ("sc_blowwood_ark4ip_1024", "fp64", 4),
+    ("gain_ark4ip_1024", "fp64", 2), ("sc_hollenbeck_ark4ip_2048", "fp64", 2),
+    ("soliton_n2_1024", "fp32", 2), ("sc_blowwood_fixed_4096", "fp32", 2),
+    ("sc_blowwood_fixed_4096", "fp32", 4)])
+def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
+    case = gc.load(name)
+    _, out, st = run(case, precision, cluster)
+    assert st["status"] == 0
+    if precision == "fp64":
+        assert st["evals"] == len(case["rk4ip_calls"])
+        assert rel_l2(out, case["A_out"]) <= FP64_TOL
+    else:
+        assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
+
+
+def test_fixed_step_traces(cuda_ready):
+    case = gc.load("soliton_n2_1024")
+    plan = make_plan(case, "fp64")
+    f = plan.pack([case["A0"]])
+    plan.propagate(f)
+    z, a = plan.instance_traces(0)
+    np.testing.assert_allclose(z, case["trace_z"], rtol=1e-14)
+    np.testing.assert_allclose([np.max(np.abs(x) ** 2) for x in a], case["trace_peak"], rtol=1e-9)
+
+
+def test_adaptive_traces(cuda_ready):
+    case = gc.load("sc_blowwood_ark4ip_1024")
+    plan = make_plan(case, "fp64")
+    f = plan.pack([case["A0"]])
+    plan.propagate(f)
+    z, a = plan.instance_traces(0)
+    np.testing.assert_allclose(z, case["trace_z"], rtol=1e-12)
+    np.testing.assert_allclose([np.max(np.abs(x) ** 2) for x in a], case["trace_peak"], rtol=1e-9)
+
+
+def test_sc_cfg_8192_fp64_and_fp32(cuda_ready):
+    """The single 2^13 supercontinuum run (15 cm, ARK4IP 1e-6, Raman + SS)."""
+    case = gc.load("sc_cfg_8192")
+    _, out64, st64 = run(case, "fp64")
+    assert st64["status"] == 0
+    assert st64["evals"] == len(case["rk4ip_calls"])
+    assert rel_l2(out64, case["A_out"]) <= FP64_TOL
+    _, out32, st32 = run(case, "fp32")
+    assert st32["status"] == 0
+    assert spec_err(out32, case["A_out"]) <= FP32_SPEC_TOL
+
+
+def test_known_answer_soliton_peak(cuda_ready):
+    """pyofss/tests/test_solver.py:278-284 on the engine: peak power 4 to 5 decimals."""
+    case = gc.load("soliton_test_solver_2048")
+    for prec in ("fp64", "fp32"):
+        _, out, _ = run(case, prec)
+        np.testing.assert_almost_equal(np.max(np.abs(out) ** 2), 4.0, 5 if prec == "fp64" else 4)
+
+
+def test_resume_in_chunks_is_identical(cuda_ready):
+    """Checkpoint/resume: a run split into attempt budgets equals the single run."""
+    case = gc.load("sc_blowwood_ark4ip_1024")
+    plan = make_plan(case, "fp64")
+    f1 = plan.pack([case["A0"]])
+    plan.propagate(f1)
+    ref = f1.cpu().numpy()
+    f2 = plan.pack([case["A0"]])
+    plan.reset()
+    for _ in range(1000):
+        plan.propagate(f2, max_attempts=7, reset=False)
+        if plan.stats()[0]["finished"]:
+            break
+    assert plan.stats()[0]["finished"] == 1
+    np.testing.assert_array_equal(f2.cpu().numpy(), ref)
+
+
+def test_host_entry_point_matches_device(cuda_ready):
+    case = gc.load("ss_only_ark4ip_1024")
+    plan = make_plan(case, "fp32")
+    f = plan.pack([case["A0"]])
+    plan.propagate(f)
+    dev = f.cpu().numpy()
+    host = plan.propagate_host(case["A0"].astype(np.complex64))
+    np.testing.assert_array_equal(host, dev)
+
+
+def test_nonfinite_input_reports_small_step(cuda_ready):
+    """Fault injected on the host: a NaN sample drives delta = 1 and h -> 0."""
+    case = gc.load("ss_only_ark4ip_1024")
+    a0 = case["A0"].copy()
+    a0[10] = np.nan
+    plan = make_plan(case, "fp32")
+    f = plan.pack([a0])
+    plan.propagate(f)
+    st = plan.stats()[0]
+    assert st["status"] == 1  # SmallStepSizeError
+    assert st["finished"] == 1

@@ -1,0 +1,106 @@
+"""Host-side mirror of the pyofss interface: grids, pulses, operator tables, ABI."""
+
+import ctypes as ct
+import os
+import re
+import shutil
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from oracle import gnlse_oracle as go
+from pyofsschanged_gb300 import Domain, Gaussian, Sech
+from pyofsschanged_gb300 import field as pf
+from pyofsschanged_gb300.operators import GridTables
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("kw", [dict(bit_width=32.0, samples_per_bit=1024),
+                                dict(bit_width=12.5, samples_per_bit=8192, centre_nu=359.0),
+                                dict(total_bits=4, bit_width=25.0, samples_per_bit=512)])
+def test_domain_matches_oracle(kw):
+    d, g = Domain(**kw), go.Grid(**kw)
+    for a in ("t", "nu", "omega", "Lambda"):
+        np.testing.assert_array_equal(getattr(d, a), getattr(g, a))
+    assert d.dt == g.dt and d.window_t == g.window_t and d.centre_omega == g.centre_omega
+
+
+def test_domain_range_checks():
+    from pyofsschanged_gb300.domain import OutOfRangeError
+    with pytest.raises(OutOfRangeError):
+        Domain(centre_nu=100.0)
+    with pytest.raises(OutOfRangeError):
+        Domain(samples_per_bit=0)
+
+
+@pytest.mark.parametrize("name", [n for n in gc.names() if n != "sc_cfg_8192"])
+def test_pulses_match_reference_fixture(name):
+    case = gc.load(name)
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    p = dict(prm["pulse"])
+    cls = Sech if p.pop("kind") == "sech" else Gaussian
+    a0 = cls(**p)(d, np.zeros(d.total_samples, complex))
+    np.testing.assert_array_equal(a0, case["A0"])
+
+
+def test_operator_tables_match_oracle():
+    case = gc.load("gain_ark4ip_1024")
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    fk = gc.fibre_kwargs(prm)
+    for k in ("method", "local_error", "traces", "total_steps"):
+        fk.pop(k, None)
+    g = GridTables(d, beta=fk["beta"], gamma=fk["gamma"], self_steepening=True,
+                   use_all="blowwood", small_signal_gain=fk["small_signal_gain"],
+                   E_sat=fk["E_sat"], length=fk["length"], lamb0=fk["lamb0"],
+                   bandwidth=fk["bandwidth"])
+    p = go.Propagator(go.Grid(**gc.domain_kwargs(prm)), **fk)
+    np.testing.assert_allclose(g.beta_w, p.factor.imag, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(g.hR_re + 1j * g.hR_im, p.nl.h_R, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(g.ss_w, 1.0 + p.nl.omega * p.nl.ss_factor, rtol=1e-15)
+    np.testing.assert_allclose(g.gain_profile, p.gain.profile, rtol=1e-15)
+    assert g.gain_log == p.gain.gain_log
+
+
+def test_hollenbeck_table_matches_oracle():
+    d = Domain(bit_width=12.5, samples_per_bit=2048, centre_nu=359.0)
+    g = GridTables(d, beta=[0, 0, -1.0], gamma=1.0, use_all="hollenbeck")
+    nl = go.Nonlinear(go.Grid(bit_width=12.5, samples_per_bit=2048, centre_nu=359.0), 1.0,
+                      use_all="hollenbeck")
+    np.testing.assert_allclose(g.hR_re + 1j * g.hR_im, nl.h_R, rtol=1e-12, atol=1e-12)
+
+
+def test_field_helpers_convention():
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal(64) + 1j * rng.standard_normal(64)
+    np.testing.assert_allclose(pf.fft(a), go.fft(a), atol=1e-14)
+    np.testing.assert_allclose(pf.ifft(pf.fft(a)), a, atol=1e-13)
+    t = np.linspace(-1, 1, 64, endpoint=False)
+    assert abs(pf.energy(a, t) - go.energy(a, t)) < 1e-14
+
+
+def _header_symbols():
+    src = open(os.path.join(ROOT, "include", "gnlse.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(gnlse_\w+)\s*\(", src,
+                                 re.M)))
+
+
+def test_abi_library_exports_every_declared_symbol():
+    from pyofsschanged_gb300 import _native
+    lib_path = _native.LIB_PATH
+    if not os.path.exists(lib_path):
+        if shutil.which("nvcc") is None:
+            pytest.skip("libgnlse.so not built and no nvcc")
+        from pyofsschanged_gb300 import build
+        build.build()
+    lib = ct.CDLL(lib_path)
+    syms = _header_symbols()
+    assert len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(_native.SIGNATURES)
+    lib.gnlse_abi_version.restype = ct.c_int
+    assert lib.gnlse_abi_version() == 1
