@@ -1,0 +1,382 @@
+"""GNLSE ensemble benchmark: solves/s of the ragged supercontinuum ensemble on one GB300.
+
+A step is one complete solve of the 256-member noise ensemble (2^12 / 2^13 /
+2^14-point grids, 5-20 cm, 2-15 kW, 30-120 fs sech + one photon per mode,
+ARK4IP at 1e-6) through the fused engine.  ``value`` is whole-job solves/s with
+the inputs resident in HBM (each step restores the inputs device-to-device,
+resets the per-member state and propagates every member to its fibre end);
+``e2e`` is the same metric through the C ABI's host-buffer entry point
+(host->device copy of the inputs and device->host copy of the outputs inside
+the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
+    python bench.py --impl reference ...   # the CPU reference path (FP64 oracle), all cores
+"""
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GNLSE ensemble solves/s on 1 GB300 (fused vs plain, <=1e-4 rel spectral err)"
+UNIT = "solves/s"
+WORKLOAD = "sc_ensemble_256_ragged_2^12-2^14_ark4ip_1e-6"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--accuracy-members", type=int, default=12,
+                    help="members re-solved in FP64 on the GPU to state the spectral error")
+    ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-attempts", type=int, default=0,
+                    help="profiling only: run W+K launches of at most this many attempts per "
+                         "member and exit (short kernels for ncu); prints no bench line")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------
+# CPU reference path (FP64 oracle restatement of pyofss ARK4IP), bounded samples
+# ----------------------------------------------------------------------------
+def _cpu_attempts_worker(args):
+    member, n_members, attempts = args
+    import numpy as np  # noqa: F401
+    from oracle import gnlse_oracle as go
+    from pyofsschanged_gb300.ensemble import FIBRE_835, sc_ensemble
+    members, domains, fields = sc_ensemble(n_members)
+    m = members[member]
+    d = domains[m.n]
+    grid = go.Grid(bit_width=d.bit_width, samples_per_bit=d.samples_per_bit, centre_nu=d.centre_nu)
+    p = go.Propagator(grid, m.length, **FIBRE_835)
+    t0 = time.perf_counter()
+    _, info = p.adaptive(fields[member].copy(), 1e-6, max_attempts=attempts)
+    return m.n, info["attempts"], time.perf_counter() - t0
+
+
+def cpu_sample(n_members, cores, budget_s, attempts_per_member=None):
+    """Time the oracle on all `cores` at once: per-attempt seconds for each grid size."""
+    from pyofsschanged_gb300.ensemble import sc_ensemble
+    members, _, _ = sc_ensemble(n_members)
+    by_n = {}
+    for i, m in enumerate(members):
+        by_n.setdefault(m.n, []).append(i)
+    # per-attempt cost on one core ~ 3 evals x (1.1, 2.4, 8.4) ms at 2^12, 2^13, 2^14
+    est = {4096: 3 * 1.2e-3, 8192: 3 * 2.6e-3, 16384: 3 * 9.0e-3}
+    jobs = []
+    sizes = sorted(by_n)
+    for k in range(cores):
+        n = sizes[k % len(sizes)]
+        mem = by_n[n][(k // len(sizes)) % len(by_n[n])]
+        att = attempts_per_member or max(4, int(budget_s / est.get(n, 0.03)))
+        jobs.append((mem, n_members, att))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_attempts_worker, jobs)
+    wall = time.perf_counter() - t0
+    per_att = {}
+    for n, att, sec in res:
+        per_att.setdefault(n, []).append(sec / max(att, 1))
+    per_att = {n: statistics.median(v) for n, v in per_att.items()}
+    total_att = sum(a for _, a, _ in res)
+    return per_att, wall, total_att, jobs
+
+
+def cpu_solves_per_s(per_att, attempts_by_member, sizes_by_member, cores):
+    """Whole-machine solves/s: `cores` independent solves at the sampled per-attempt cost."""
+    t_solves = [attempts_by_member[i] * per_att[sizes_by_member[i]] for i in range(len(sizes_by_member))]
+    mean_t = sum(t_solves) / len(t_solves)
+    return cores / mean_t
+
+
+def load_costs(n_members):
+    path = os.path.join(ROOT, "tests", "golden", "ensemble_costs.json")
+    with open(path) as f:
+        c = json.load(f)
+    res = c["results"]
+    if len(res) < n_members:
+        raise RuntimeError("ensemble_costs.json covers fewer members than requested")
+    return [r["attempts"] for r in res[:n_members]], [r["n"] for r in res[:n_members]]
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    attempts, sizes = load_costs(a.members)
+    values = []
+    per_step = max(2.0, a.cpu_sample_s / 2)
+    for s in range(a.warmup + a.steps):
+        per_att, wall, tot, jobs = cpu_sample(a.members, cores, per_step)
+        if s >= a.warmup:
+            values.append(cpu_solves_per_s(per_att, attempts, sizes, cores))
+    v = statistics.median(values)
+    sample = (f"per step: {cores} oracle processes (one per core) each ran a bounded number of "
+              f"ARK4IP attempts (~{per_step:.0f} s) of one ensemble member; per-attempt cost per "
+              f"grid size x the members' full attempt counts (tests/golden/ensemble_costs.json)")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * a.members / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "members": a.members},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    cpu_line = None
+    from pyofsschanged_gb300.engine import Plan
+    from pyofsschanged_gb300.ensemble import ensemble_plan_inputs, sc_ensemble
+
+    members, domains, fields = sc_ensemble(a.members)
+    grids, inst = ensemble_plan_inputs(members, domains)
+    plan = Plan(grids, inst, precision=a.precision, device=local)
+    src = plan.pack(fields)
+    work = torch.empty_like(src)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def step():
+        work.copy_(src)
+        plan.propagate(work, stream=stream)
+        flush.fill_(1.0)  # write > L2 between steps
+
+    if a.profile_attempts > 0:
+        work.copy_(src)
+        plan.reset(stream)
+        for _ in range(a.warmup + a.steps):
+            plan.propagate(work, max_attempts=a.profile_attempts, stream=stream, reset=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_attempts": a.profile_attempts, "launches": a.warmup + a.steps,
+                          "classes": len(plan.class_times())}))
+        return 0
+
+    plan.set_timing(True)
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    stats_w = plan.stats()
+    clocks = ClockSampler(local)
+    class_ms = []
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        step()
+        class_ms.append(plan.class_times())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    barrier()
+    ms_total = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    stats = plan.stats()
+    assert all(s["status"] == 0 and s["finished"] for s in stats), "a member did not finish"
+    ms_step = ms_total / a.steps
+    value = world * a.members * a.steps / (ms_total * 1e-3)
+
+    # roofline of the dominant kernel (largest share of kernel time)
+    n_by_cls = {}
+    for i, s in enumerate(stats):
+        g = plan.grids[plan.instances[i].grid]
+        n_by_cls.setdefault(g.n, 0)
+        n_by_cls[g.n] += s["evals"] * 2 * g.n * (8 if a.precision == "fp32" else 16)
+    per_cls = {}
+    for step_times in class_ms:
+        for (logm, c, cnt, ms) in step_times:
+            per_cls.setdefault((logm, c, cnt), []).append(ms)
+    dom = max(per_cls, key=lambda k: sum(per_cls[k]))
+    dom_ms = statistics.mean(per_cls[dom])
+    dom_n = (1 << dom[0]) * dom[1]
+    alg_bytes = n_by_cls[dom_n]
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+    fft_flops = 0.0
+    for i, s in enumerate(stats):
+        n = plan.grids[plan.instances[i].grid].n
+        if n == dom_n:
+            fft_flops += s["evals"] * 16 * 5.0 * n * math.log2(n)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "kernel": f"gnlse_kernel<{'double' if a.precision == 'fp64' else 'float'},{dom[0]},{dom[1]},{'true' if a.precision == 'mixed' else 'false'}>",
+                "launch_ms": dom_ms, "alg_bytes_per_launch": alg_bytes,
+                "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback",
+                "fft_gflops": fft_flops / (dom_ms * 1e-3) / 1e9}
+
+    # end to end through the C ABI host-buffer entry point
+    npdt = np.complex64 if a.precision == "fp32" else np.complex128
+    host_in = src.cpu().numpy().astype(npdt)
+    host_out = np.empty_like(host_in)
+    plan.propagate_host(host_in, host_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        plan.propagate_host(host_in, host_out)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * a.members * a.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes)}
+
+    # spectral error of the timed precision against FP64 on the same inputs
+    acc = None
+    if a.accuracy_members > 0 and rank == 0:
+        idx = list(range(min(a.accuracy_members, a.members)))
+        sub_m = [members[i] for i in idx]
+        g64, i64 = ensemble_plan_inputs(sub_m, {n: domains[n] for n in set(m.n for m in sub_m)})
+        p64 = Plan(g64, i64, precision="fp64", device=local)
+        f64 = p64.pack([fields[i] for i in idx])
+        p64.propagate(f64)
+        ref = [x.cpu().numpy() for x in p64.unpack(f64)]
+        out = [x.cpu().numpy().astype(complex) for x in plan.unpack(work)]
+        errs = []
+        for j, i in enumerate(idx):
+            s_ref = np.fft.ifft(ref[j])
+            s_out = np.fft.ifft(out[i])
+            errs.append(float(np.linalg.norm(s_out - s_ref) / np.linalg.norm(s_ref)))
+        acc = {"members": len(idx), "median": statistics.median(errs), "max": max(errs),
+               "frac_le_1e-4": sum(e <= 1e-4 for e in errs) / len(errs)}
+
+    if rank == 0 and not a.no_cpu:
+        per_att, wall, tot, jobs = cpu_sample(a.members, os.cpu_count() or 1, a.cpu_sample_s)
+        attempts = [s["attempts"] for s in stats]
+        sizes = [plan.grids[plan.instances[i].grid].n for i in range(len(stats))]
+        cores = os.cpu_count() or 1
+        v = cpu_solves_per_s(per_att, attempts, sizes, cores)
+        cpu_line = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                    "sample": (f"{cores} concurrent oracle (FP64 numpy restatement of pyofss "
+                               f"ARK4IP) processes, {tot} attempts in {wall:.1f} s; per-attempt "
+                               f"cost per grid size x this run's per-member attempt counts")}
+    launches = a.steps * len(class_ms[0])
+    evals = sum(s["evals"] for s in stats)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "c64", "mixed": "c64+df-state", "fp64": "c128"}[a.precision], "data": "synthetic",
+            "config": {"workload": WORKLOAD, "members": a.members, "precision": a.precision,
+                       "grids": "2^12/2^13/2^14 mixed, dt=12.5ps/8192, 835 nm",
+                       "l2": "256 MiB buffer written between steps",
+                       "evals_per_step": evals},
+            "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
+            "gpu_launches": launches, "accuracy_vs_fp64": acc,
+            "class_ms": {f"m2^{k[0]}_c{k[1]}_n{k[2]}": statistics.mean(v) for k, v in per_cls.items()}}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

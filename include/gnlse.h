@@ -28,7 +28,8 @@
  * Conventions: units as pyofss (t ps, nu THz, omega rad/ps, z km, beta_k
  * ps^k/km, gamma 1/(W km), power W, energy nJ).  Fields are complex
  * (interleaved re, im) in the time domain, natural order (t from -T/2),
- * complex64 for GNLSE_FP32 plans and complex128 for GNLSE_FP64 plans.
+ * complex64 for GNLSE_FP32 plans and complex128 for GNLSE_FP64 and
+ * GNLSE_MIXED plans.
  * Spectral tables are in FFT order (pyofss fftshift order).
  *
  * All device pointers are plain CUDA device pointers; stream arguments are
@@ -60,7 +61,12 @@ enum {
 };
 
 enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1 };
-enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1 };
+/* precision: GNLSE_FP32 complex64 throughout (fields complex64);
+ * GNLSE_FP64 complex128 throughout (fields complex128);
+ * GNLSE_MIXED complex64 transforms and nonlinear evaluations with the
+ * propagation state, RK accumulator and exp(hD) factors in double-float
+ * (about 48 bits) and FP64 input/output transforms (fields complex128). */
+enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1, GNLSE_MIXED = 2 };
 
 /* One grid (pyofss Domain) with the fibre operators built on it. */
 typedef struct {
@@ -119,8 +125,7 @@ int gnlse_abi_version(void);
 const char* gnlse_status_string(int status);
 
 /* Build device tables and scratch for n_instances propagations over n_grids
- * grids.  precision: GNLSE_FP32 (complex64 state, FP64 phase and control) or
- * GNLSE_FP64 (complex128 throughout). */
+ * grids with the given precision (GNLSE_FP32, GNLSE_FP64 or GNLSE_MIXED). */
 int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids,
                       int n_instances, const gnlse_instance_desc* instances,
                       gnlse_plan** plan_out);
@@ -152,6 +157,16 @@ int gnlse_propagate(gnlse_plan* plan, void* d_fields, void* d_traces, double* d_
 /* Same, from and to host memory: copies the fields in, propagates to the end
  * and copies the fields out (synchronous).  h_in and h_out may alias. */
 int gnlse_propagate_host(gnlse_plan* plan, const void* h_in, void* h_out, void* stream);
+
+/* Kernel timing.  With timing enabled every propagate records CUDA events
+ * around each launch class (one kernel launch per distinct points-per-CTA and
+ * cluster size) on the stream that class is launched on.  gnlse_class_times
+ * waits for the last propagate's events and reports, per class, log2 of the
+ * points per CTA, the cluster size, the number of instances and the kernel
+ * duration in ms; it returns the number of classes (or a negative status). */
+int gnlse_set_timing(gnlse_plan* plan, int enable);
+int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t* cluster,
+                      int32_t* count, double* ms);
 
 /* Copy per-instance statistics to host memory (synchronises `stream`). */
 int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);

@@ -9,7 +9,7 @@ import os
 import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgnlse.so")
+LIB_PATH = os.environ.get("GNLSE_LIB", os.path.join(HERE, "libgnlse.so"))
 
 GNLSE_OK = 0
 GNLSE_SMALL_STEP = 1
@@ -25,6 +25,7 @@ GNLSE_RK4IP = 0
 GNLSE_ARK4IP = 1
 GNLSE_FP32 = 0
 GNLSE_FP64 = 1
+GNLSE_MIXED = 2
 
 _dp = ct.POINTER(ct.c_double)
 
@@ -83,6 +84,10 @@ SIGNATURES = {
                                    ct.c_int64, ct.c_void_p]),
     "gnlse_propagate_host": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "gnlse_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
+    "gnlse_set_timing": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
+                                     ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
+                                     ct.POINTER(ct.c_double)]),
 }
 
 _lib = None

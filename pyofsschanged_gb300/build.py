@@ -17,13 +17,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(CSRC, "_build")
-LIB = os.path.join(HERE, "libgnlse.so")
+_TAG = os.environ.get("GNLSE_BUILD_TAG", "")
+BUILD = os.path.join(CSRC, "_build" + (("_" + _TAG) if _TAG else ""))
+LIB = os.path.join(HERE, "libgnlse%s.so" % (("_" + _TAG) if _TAG else ""))
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE]
+              "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE] + \
+    os.environ.get("GNLSE_NVCC_FLAGS", "").split()
 
 
 def nvcc():
@@ -59,6 +61,10 @@ def _compile(src, obj):
 def build(jobs=None, force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    units = os.environ.get("GNLSE_UNITS")  # optional regex: build a subset of units
+    if units:
+        import re
+        srcs = [s for s in srcs if re.search(units, os.path.basename(s))]
     hdr = max([os.path.getmtime(h) for h in _headers()] + [0.0])
     todo, objs = [], []
     for s in srcs:

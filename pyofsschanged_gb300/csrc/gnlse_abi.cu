@@ -31,23 +31,40 @@ struct GridHost {
   void* d_lor = nullptr;
   void* d_nu = nullptr;
   void* d_tw = nullptr;
+  void* d_twl = nullptr;
+  void* d_tw64 = nullptr;
+  void* d_twl64 = nullptr;
+  void* d_cis = nullptr;
 };
 
 bool supported(int precision, int logm, int C) {
-#define GNLSE_MATCH(R, L, CC) \
-  if ((sizeof(R) == 8) == (precision == GNLSE_FP64) && logm == (L) && C == (CC)) return true;
-  GNLSE_CLASSES_F32(GNLSE_MATCH)
-  GNLSE_CLASSES_F64(GNLSE_MATCH)
+#define GNLSE_MATCH(PREC, R, L, CC) \
+  if (precision == (PREC) && logm == (L) && C == (CC)) return true;
+#define GNLSE_M32(R, L, CC) GNLSE_MATCH(GNLSE_FP32, R, L, CC)
+#define GNLSE_M64(R, L, CC) GNLSE_MATCH(GNLSE_FP64, R, L, CC)
+#define GNLSE_MMX(R, L, CC) GNLSE_MATCH(GNLSE_MIXED, R, L, CC)
+  GNLSE_CLASSES_F32(GNLSE_M32)
+  GNLSE_CLASSES_F64(GNLSE_M64)
+  GNLSE_CLASSES_MIX(GNLSE_MMX)
+#undef GNLSE_M32
+#undef GNLSE_M64
+#undef GNLSE_MMX
 #undef GNLSE_MATCH
   return false;
 }
 
 cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, cudaStream_t s) {
-#define GNLSE_CALL(R, L, CC)                                                     \
-  if ((sizeof(R) == 8) == (precision == GNLSE_FP64) && logm == (L) && C == (CC)) \
-    return launch_class<R, L, CC>(kp, n, s);
-  GNLSE_CLASSES_F32(GNLSE_CALL)
-  GNLSE_CLASSES_F64(GNLSE_CALL)
+#define GNLSE_CALL(PREC, XS, R, L, CC) \
+  if (precision == (PREC) && logm == (L) && C == (CC)) return launch_class<R, L, CC, XS>(kp, n, s);
+#define GNLSE_C32(R, L, CC) GNLSE_CALL(GNLSE_FP32, false, R, L, CC)
+#define GNLSE_C64(R, L, CC) GNLSE_CALL(GNLSE_FP64, false, R, L, CC)
+#define GNLSE_CMX(R, L, CC) GNLSE_CALL(GNLSE_MIXED, true, R, L, CC)
+  GNLSE_CLASSES_F32(GNLSE_C32)
+  GNLSE_CLASSES_F64(GNLSE_C64)
+  GNLSE_CLASSES_MIX(GNLSE_CMX)
+#undef GNLSE_C32
+#undef GNLSE_C64
+#undef GNLSE_CMX
 #undef GNLSE_CALL
   return cudaErrorInvalidValue;
 }
@@ -62,7 +79,8 @@ int ilog2i(int n) {
 
 struct gnlse_plan {
   int precision = 0;
-  size_t vsize = 8;
+  size_t vsize = 8;    // bytes per field element
+  size_t ssize = 8;    // bytes per scratch element
   int device = 0;
   std::vector<GridHost> grids;
   std::vector<InstDev> inst;
@@ -79,6 +97,8 @@ struct gnlse_plan {
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> ev;
   cudaEvent_t fork = nullptr;
+  bool timing = false;
+  std::vector<cudaEvent_t> t0, t1;
   // host-buffer entry point staging
   void* d_io = nullptr;
   void* d_tr = nullptr;
@@ -102,12 +122,13 @@ cudaError_t upload(gnlse_plan* p, const std::vector<T>& h, void** d) {
 }
 
 template <class R>
-cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost& gh, GridDev& dv) {
+cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost& gh, GridDev& dv,
+                              bool extended) {
   const int n = gd.n, C = gh.C, M = n / C;
   auto perm = [&](int a) { return (a % M) * C + a / M; };  // slot a = c*M + k2  <-  k = c + C*k2
   std::vector<double> beta(n), nu(n);
   std::vector<R> Kr(n), lor, Hp;
-  std::vector<R> tw(2 * (size_t)n);
+  std::vector<R> tw(2 * (size_t)n), twl(2 * (size_t)M);
   for (int a = 0; a < n; ++a) {
     const int k = perm(a);
     beta[a] = gd.beta_w[k];
@@ -127,13 +148,46 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
     lor.resize(n);
     for (int a = 0; a < n; ++a) lor[a] = (R)(gd.gain_profile ? gd.gain_profile[perm(a)] : 1.0);
   }
-  // exp(+2 pi i j / n): reduce j to the first octant for an accurate argument
+  // exp(+2 pi i j / n), argument formed in long double
   for (int j = 0; j < n; ++j) {
     const long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)j / (long double)n;
     tw[2 * (size_t)j] = (R)std::cos((double)ang);
     tw[2 * (size_t)j + 1] = (R)std::sin((double)ang);
   }
+  for (int j = 0; j < M; ++j) {
+    twl[2 * (size_t)j] = tw[2 * (size_t)j * C];
+    twl[2 * (size_t)j + 1] = tw[2 * (size_t)j * C + 1];
+  }
   cudaError_t e;
+  if (extended) {
+    // FP64 twiddles for the boundary transforms and the double-float
+    // cis(j pi/512) table of the exp(hD) factors
+    std::vector<double> tw64(2 * (size_t)n), twl64(2 * (size_t)M);
+    std::vector<float> cis(4 * 1024);
+    const long double PI_L = 3.14159265358979323846264338327950288L;
+    for (int j = 0; j < n; ++j) {
+      const long double ang = 2.0L * PI_L * (long double)j / (long double)n;
+      tw64[2 * (size_t)j] = (double)std::cos((double)ang);
+      tw64[2 * (size_t)j + 1] = (double)std::sin((double)ang);
+    }
+    for (int j = 0; j < M; ++j) {
+      twl64[2 * (size_t)j] = tw64[2 * (size_t)j * C];
+      twl64[2 * (size_t)j + 1] = tw64[2 * (size_t)j * C + 1];
+    }
+    for (int j = 0; j < 1024; ++j) {
+      const long double ang = PI_L * (long double)j / 512.0L;
+      const long double c = cosl(ang), sn = sinl(ang);
+      const float ch = (float)c, sh = (float)sn;
+      cis[4 * j + 0] = ch;
+      cis[4 * j + 1] = sh;
+      cis[4 * j + 2] = (float)(c - (long double)ch);
+      cis[4 * j + 3] = (float)(sn - (long double)sh);
+    }
+    if ((e = upload(p, tw64, &gh.d_tw64)) != cudaSuccess) return e;
+    if ((e = upload(p, twl64, &gh.d_twl64)) != cudaSuccess) return e;
+    if ((e = upload(p, cis, &gh.d_cis)) != cudaSuccess) return e;
+  }
+  if ((e = upload(p, twl, &gh.d_twl)) != cudaSuccess) return e;
   if ((e = upload(p, beta, &gh.d_beta)) != cudaSuccess) return e;
   if ((e = upload(p, nu, &gh.d_nu)) != cudaSuccess) return e;
   if ((e = upload(p, Kr, &gh.d_Kr)) != cudaSuccess) return e;
@@ -146,6 +200,10 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   dv.lor = gd.gain_on ? gh.d_lor : nullptr;
   dv.nu = (const double*)gh.d_nu;
   dv.tw = gh.d_tw;
+  dv.twl = gh.d_twl;
+  dv.tw64 = gh.d_tw64;
+  dv.twl64 = gh.d_twl64;
+  dv.cis_df = gh.d_cis;
   dv.n = n;
   dv.logm = gh.logm;
   dv.C = C;
@@ -165,6 +223,8 @@ void free_plan(gnlse_plan* p) {
   for (void* a : p->allocs) cudaFree(a);
   for (auto s : p->side) cudaStreamDestroy(s);
   for (auto e : p->ev) cudaEventDestroy(e);
+  for (auto e : p->t0) cudaEventDestroy(e);
+  for (auto e : p->t1) cudaEventDestroy(e);
   if (p->fork) cudaEventDestroy(p->fork);
   delete p;
 }
@@ -193,12 +253,14 @@ const char* gnlse_status_string(int s) {
 int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, int n_instances,
                       const gnlse_instance_desc* instances, gnlse_plan** plan_out) {
   if (!plan_out || !grids || !instances || n_grids <= 0 || n_instances <= 0) return GNLSE_BAD_ARGUMENT;
-  if (precision != GNLSE_FP32 && precision != GNLSE_FP64) return GNLSE_BAD_ARGUMENT;
+  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED)
+    return GNLSE_BAD_ARGUMENT;
   *plan_out = nullptr;
   gnlse_plan* p = new (std::nothrow) gnlse_plan();
   if (!p) return GNLSE_OUT_OF_MEMORY;
   p->precision = precision;
-  p->vsize = precision == GNLSE_FP64 ? 16 : 8;
+  p->vsize = precision == GNLSE_FP32 ? 8 : 16;
+  p->ssize = precision == GNLSE_FP32 ? 8 : 16;
   cudaGetDevice(&p->device);
   std::vector<GridDev> gdev(n_grids);
   p->grids.resize(n_grids);
@@ -211,8 +273,13 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       return GNLSE_BAD_ARGUMENT;
     }
     int C = gd.cluster;
-    const int mmax = precision == GNLSE_FP64 ? 4096 : 8192;
-    if (C == 0) C = n <= mmax ? 1 : n / mmax;
+    // points per CTA: 4096 (complex64: 3 CTAs of 256 threads fit one SM) or
+    // 4096 (complex128: one CTA per SM); larger grids span a cluster
+    const int mmax = 4096;
+    if (C == 0) {
+      C = n <= mmax ? 1 : n / mmax;
+      if (C > 8) C = n / (2 * mmax);  // complex64 2^16: 8 CTAs of 8192 points
+    }
     if (C != 1 && C != 2 && C != 4 && C != 8) {
       free_plan(p);
       return GNLSE_UNSUPPORTED;
@@ -226,8 +293,9 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     gh.n = n;
     gh.logm = logm;
     gh.C = C;
-    cudaError_t e = precision == GNLSE_FP64 ? build_grid_tables<double>(p, gd, gh, gdev[i])
-                                            : build_grid_tables<float>(p, gd, gh, gdev[i]);
+    cudaError_t e = precision == GNLSE_FP64
+                        ? build_grid_tables<double>(p, gd, gh, gdev[i], false)
+                        : build_grid_tables<float>(p, gd, gh, gdev[i], precision == GNLSE_MIXED);
     if (e != cudaSuccess) {
       free_plan(p);
       return cuda_fail(e);
@@ -277,7 +345,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   p->field_elems = foff;
   p->trace_elems = toff;
   p->tracez_elems = zoff;
-  p->scratch_bytes = (size_t)soff * p->vsize;
+  p->scratch_bytes = (size_t)soff * p->ssize;
   // classes: instances grouped by (logm, C), longest estimated work first
   std::vector<int> ids(n_instances);
   for (int i = 0; i < n_instances; ++i) ids[i] = i;
@@ -322,6 +390,13 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     }
     p->side.push_back(s);
     p->ev.push_back(ev);
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+      free_plan(p);
+      return GNLSE_CUDA_ERROR;
+    }
+    p->t0.push_back(a);
+    p->t1.push_back(b);
   }
   if (cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) != cudaSuccess) {
     free_plan(p);
@@ -378,8 +453,11 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     const ClassRun& c = p->classes[0];
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
+    if (p->timing && (e = cudaEventRecord(p->t0[0], s)) != cudaSuccess) return cuda_fail(e);
     e = dispatch(p->precision, c.logm, c.C, kp, c.count, s);
-    return e == cudaSuccess ? GNLSE_OK : cuda_fail(e);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecord(p->t1[0], s)) != cudaSuccess) return cuda_fail(e);
+    return GNLSE_OK;
   }
   // several classes: fork onto side streams so they share the GPU, then join
   if ((e = cudaEventRecord(p->fork, s)) != cudaSuccess) return cuda_fail(e);
@@ -388,7 +466,9 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     if ((e = cudaStreamWaitEvent(p->side[k], p->fork, 0)) != cudaSuccess) return cuda_fail(e);
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
+    if (p->timing && (e = cudaEventRecord(p->t0[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecord(p->t1[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaEventRecord(p->ev[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaStreamWaitEvent(s, p->ev[k], 0)) != cudaSuccess) return cuda_fail(e);
   }
@@ -418,6 +498,31 @@ int gnlse_propagate_host(gnlse_plan* p, const void* h_in, void* h_out, void* str
   if ((e = cudaMemcpyAsync(h_out, p->d_io, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_fail(e);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
   return GNLSE_OK;
+}
+
+int gnlse_set_timing(gnlse_plan* p, int enable) {
+  if (!p) return GNLSE_BAD_ARGUMENT;
+  p->timing = enable != 0;
+  return GNLSE_OK;
+}
+
+int gnlse_class_times(gnlse_plan* p, int max_classes, int32_t* logm, int32_t* cluster,
+                      int32_t* count, double* ms) {
+  if (!p || max_classes < 0) return -GNLSE_BAD_ARGUMENT;
+  const int nc = (int)p->classes.size();
+  for (int k = 0; k < nc && k < max_classes; ++k) {
+    float t = 0.f;
+    if (p->timing) {
+      if (cudaEventSynchronize(p->t1[k]) != cudaSuccess ||
+          cudaEventElapsedTime(&t, p->t0[k], p->t1[k]) != cudaSuccess)
+        return -GNLSE_CUDA_ERROR;
+    }
+    if (logm) logm[k] = p->classes[k].logm;
+    if (cluster) cluster[k] = p->classes[k].C;
+    if (count) count[k] = p->classes[k].count;
+    if (ms) ms[k] = p->timing ? (double)t : 0.0;
+  }
+  return nc;
 }
 
 int gnlse_get_stats(gnlse_plan* p, gnlse_stats* out, void* stream) {

@@ -22,7 +22,17 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "gnlse_df.cuh"
 #include "gnlse_types.h"
+
+#ifndef GNLSE_MINB_CAP
+#define GNLSE_MINB_CAP 2
+#endif
+#ifndef GNLSE_RAMAN_SPLIT
+#define GNLSE_RAMAN_SPLIT 0
+#endif
 
 namespace cg = cooperative_groups;
 
@@ -113,22 +123,15 @@ __device__ __forceinline__ double simpson_w(int n, int N) {
   return (n & 1) ? 4.0 / 3.0 : 2.0 / 3.0;
 }
 
-// What the prologue of a nonlinear evaluation reads and what its epilogue
-// writes (selected at run time so the transform code is compiled once).
-enum StageKind : int {
-  SK_MA = 0,   // in: Z = S0            out: MA = i K G+(x R)          (N(A) of a state)
-  SK_S1 = 1,   // in: S_I + k0/2        out: k1 -> X, acc = S_I + k0/6 + k1/3
-  SK_S2 = 2,   // in: S_I + k1/2        out: k2 -> X, acc += k2/3
-  SK_S3 = 3,   // in: L(S_I + k2)       out: L(acc) + k3/6
-  SK_S3C = 4,  // as SK_S3, then error norms vs Sf and local extrapolation
-  SK_E_ACC = 5,  // energy of G-(acc)/N
-  SK_E_U = 6,    // energy of G-(S_I + k2)/N
-  SK_E_MA = 7    // energy of G-(MA)/N
-};
-
-template <class R, int LOGM, int C>
+// XS ("extended state"): complex64 transforms and nonlinear evaluations with
+// the propagation state, the RK accumulator and the exp(hD) factors held as
+// double-float complex values (float4) and FP64 boundary transforms.
+template <class R, int LOGM, int C, bool XS = false>
 struct Engine {
   using V = typename VT<R>::V;
+  using SV = typename std::conditional<XS, float4, V>::type;  // state-like arrays
+  using FV = typename std::conditional<XS, double2, V>::type;  // user fields / traces
+  static_assert(!XS || sizeof(R) == 4, "extended state runs on complex64 transforms");
   static constexpr int M = 1 << LOGM;
   static constexpr int N = M * C;
   static constexpr int T = (M / 16) < 64 ? 64 : (M / 16);
@@ -138,7 +141,13 @@ struct Engine {
   static constexpr int RED = 64;  // doubles of reduction scratch
   static_assert(LOGM >= 8, "M >= 256 required");
   static_assert(C == 1 || C == 2 || C == 4 || C == 8, "cluster size 1, 2, 4 or 8");
-  static constexpr size_t ctl_bytes() { return 512; }
+  static constexpr size_t ctl_bytes() { return 1024; }
+  // CTAs that fit on one SM by shared memory (228 KB per SM, 1 KB reserved per CTA)
+  static constexpr int MINB_RAW = (int)(233472 / (2 * MP * sizeof(V) + RED * sizeof(double) + 1024 + 1024));
+  // ... capped so that a thread keeps at least 64 registers (and at most
+  // GNLSE_MINB_CAP CTAs per SM are assumed when allocating registers)
+  static constexpr int MINB_REG = MINB_RAW < 1 ? 1 : (MINB_RAW * T > 1024 ? 1024 / T : MINB_RAW);
+  static constexpr int MINB = MINB_REG < GNLSE_MINB_CAP ? MINB_REG : GNLSE_MINB_CAP;
   static constexpr size_t smem_bytes() {
     return 2 * MP * sizeof(V) + RED * sizeof(double) + ctl_bytes();
   }
@@ -147,23 +156,9 @@ struct Engine {
     V* X;
     V* P;
     double* red;
-    const V* tw;
+    const V* tw;   // N-point table (cross-CTA pass)
+    const V* twl;  // M-point table (per-CTA passes)
     int rank;
-  };
-
-  // Runtime description of one nonlinear evaluation (see StageKind).
-  struct Op {
-    int kind;
-    int gain;
-    const V* S0;
-    const V* MA0;
-    const V* Et;
-    V* acc;
-    V* out;
-    const V* Sf;
-    const R* Kr;
-    const R* lor;
-    R h, aA, ak0, a3, ao;
   };
 
   static __device__ __forceinline__ V* rmt(V* p, int r) {
@@ -217,9 +212,9 @@ struct Engine {
       if (NB % T == 0 || j < NB) {
         const int k = j & (Ns - 1);
         if (Ns > 1) {
-          const int step = C * k * (M / (Ns * RAD));
+          const int step = k * (M / (Ns * RAD));
 #pragma unroll
-          for (int r = 1; r < RAD; ++r) v[b][r] = cmul(v[b][r], twid(cx.tw, r * step, SIGN));
+          for (int r = 1; r < RAD; ++r) v[b][r] = cmul(v[b][r], twid(cx.twl, r * step, SIGN));
         }
         dft<RAD, SIGN>(v[b]);
         const int base = (j - k) * RAD + k;
@@ -384,182 +379,240 @@ struct Engine {
     }
   }
 
-  // ---- stage prologue / epilogue algebra (Solver.rk4ip, solver.py:339-354) --
-  static __device__ __forceinline__ V mult(const Op& op, int a, R ga) {
-    V e = op.Et[a];
-    if (op.gain) e = cscale(e, (R)exp(ga * op.lor[a]));
+  // ---- RK4IP stage algebra (Solver.rk4ip, solver.py:339-354) ---------------
+  // Elementwise loops over this CTA's spectral slice between the transforms
+  // of consecutive stages; each loop fuses the end of one stage with the
+  // start of the next.
+  struct Op {
+    const SV* S0;
+    const V* MA0;
+    const SV* Et;
+    SV* acc;
+    SV* out;
+    const SV* Sf;
+    const R* Kr;
+    const R* lor;
+    R h, aA, ak0, a3, ao;
+    double hh;
+    int gain;
+  };
+
+  static __device__ __forceinline__ V mult(const Op& op, int a, V e, R ga) {
+    if (op.gain) e = cscale(e, (R)exp(ga * __ldg(&op.lor[a])));
     return e;
   }
   static __device__ __forceinline__ V hK(const Op& op, int a, V v) {  // h * i * K * v
-    const R k = op.h * op.Kr[a];
+    const R k = op.h * __ldg(&op.Kr[a]);
     return mk<V>(-k * v.y, k * v.x);
   }
-  static __device__ __forceinline__ V s_I(const Op& op, int a) { return cmul(mult(op, a, op.aA), op.S0[a]); }
-  static __device__ __forceinline__ V k_0(const Op& op, int a) {
-    return cscale(cmul(mult(op, a, op.ak0), op.MA0[a]), op.h);
-  }
-
-  static __device__ __forceinline__ V stage_pro(const Ctx& cx, const Op& op, int a, int l) {
-    const R half = (R)0.5;
-    switch (op.kind) {
-      case SK_MA: return op.S0[a];
-      case SK_S1: return cadd(s_I(op, a), cscale(k_0(op, a), half));
-      case SK_S2: return cadd(s_I(op, a), cscale(cx.X[pad(l)], half));
-      case SK_E_ACC: return op.acc[a];
-      case SK_E_U: return cadd(s_I(op, a), cx.X[pad(l)]);
-      case SK_E_MA: return op.MA0[a];
-      default: return cmul(mult(op, a, op.a3), cadd(s_I(op, a), cx.X[pad(l)]));  // SK_S3, SK_S3C
+  // complex64 value (or the leading part of a double-float value) of a state-like array
+  static __device__ __forceinline__ V ldv(const SV* p, int a) {
+    if constexpr (XS) {
+      return ld_hi(p, a);
+    } else {
+      return p[a];
     }
   }
-
-  static __device__ __forceinline__ void stage_fin(const Ctx& cx, const Op& op, int a, int l, V v,
-                                                   double& d2, double& f2, double& bad) {
-    const R sixth = (R)(1.0 / 6.0), third = (R)(1.0 / 3.0);
-    switch (op.kind) {
-      case SK_MA: {
-        const R k = op.Kr[a];
-        op.out[a] = mk<V>(-k * v.y, k * v.x);
-        break;
-      }
-      case SK_S1: {
-        V k1 = hK(op, a, v);
-        cx.X[pad(l)] = k1;
-        op.acc[a] = cadd(cadd(s_I(op, a), cscale(k_0(op, a), sixth)), cscale(k1, third));
-        break;
-      }
-      case SK_S2: {
-        V k2 = hK(op, a, v);
-        cx.X[pad(l)] = k2;
-        op.acc[a] = cadd(op.acc[a], cscale(k2, third));
-        break;
-      }
-      case SK_S3: {
-        V k3 = hK(op, a, v);
-        op.out[a] = cadd(cmul(mult(op, a, op.ao), op.acc[a]), cscale(k3, sixth));
-        break;
-      }
-      default: {  // SK_S3C
-        V k3 = hK(op, a, v);
-        V res = cadd(cmul(mult(op, a, op.ao), op.acc[a]), cscale(k3, sixth));
-        V sf = op.Sf[a];
-        V d = csub(sf, res);
-        d2 += (double)cabs2(d);
-        f2 += (double)cabs2(sf);
-        if (!isfinite(sf.x) || !isfinite(sf.y)) bad = 1.0;
-        // local extrapolation (stepper.py:272-274,338): (16 A_fine - A_coarse) / 15
-        const R fa = (R)(16.0 / 15.0), fb = (R)(1.0 / 15.0);
-        op.out[a] = mk<V>(fa * sf.x - fb * res.x, fa * sf.y - fb * res.y);
-        break;
-      }
-    }
+  // gain factor exp(ga * lor) as a double-float real, 1 + expm1(x)
+  static __device__ __forceinline__ dff gain_df(const Op& op, int a, R ga) {
+    return fast_two_sum(1.0f, expm1f(ga * __ldg(&op.lor[a])));
+  }
+  static __device__ __forceinline__ dfc mult_df(const Op& op, int a, dfc e, R ga) {
+    if (op.gain) e = dfc_scale(e, gain_df(op, a, ga));
+    return e;
   }
 
   // ---- the nonlinear operator ---------------------------------------------
-  // x = G-(xhat)/N for the stage input xhat; y = x R(x) with
-  // R = (1-fR)|x|^2 + fR G-(Hp G+(|x|^2)) (Raman) or |x|^2; then G+(y) is
-  // handed to the stage epilogue.  res[0] returns the Simpson energy of x
-  // (SK_MA with gain) or res[0..2] the error norms (SK_S3C).
-  static __device__ __noinline__ void nonlinear(const Ctx& cx, const GridDev& g, const Op& op_in,
-                                                double* res) {
-    const Op op = op_in;
+  // On entry X holds the stage input xhat (spectral, this CTA's slice).  With
+  // x = G-(xhat)/N and R(x) = (1-fR)|x|^2 + fR G-(Hp G+(|x|^2)) (Raman) or
+  // |x|^2, on exit X holds G+(x R(x)) (spectral).  The transforms carry only
+  // light per-element work in their first / last passes; with want_e the
+  // Simpson energy (nJ) of x is returned.
+  static __device__ __forceinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
     const R invN = (R)(1.0 / (double)N);
     const bool raman = g.raman != 0;
-    const bool want_e = (op.kind == SK_MA) && op.gain;
-    const int n_tot = N;
-    double eacc = 0.0;
     V* X = cx.X;
     V* P = cx.P;
-    auto pro = [&](int o, int l) -> V { return stage_pro(cx, op, o * M + l, l); };
+    auto rdX = [&](int o, int l) -> V { return rmt(X, o)[pad(l)]; };
+    const bool keep_p = raman || want_e;
     auto e1 = [&](int o, int l, V v) {
       V x = cscale(v, invN);
       R p = cabs2(x);
-      if (want_e) eacc += simpson_w(o * M + l, n_tot) * (double)p;
-      if (raman) {
-        rmt(X, o)[pad(l)] = x;
-        rmt(P, o)[pad(l)] = mk<V>(p, (R)0);
-      } else {
-        rmt(X, o)[pad(l)] = cscale(x, p);
-      }
+      if (keep_p) rmt(P, o)[pad(l)] = mk<V>(p, (R)0);
+      rmt(X, o)[pad(l)] = raman ? x : cscale(x, p);
     };
-    inv(cx, X, pro, e1);
+    inv(cx, X, rdX, e1);
+    double energy = 0.0;
+    if (want_e) energy = simpson_energy(cx, g, P);
     if (raman) {
       const V* Hp = (const V*)g.Hp;
       const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
       auto rdP = [&](int o, int l) -> V { return rmt(P, o)[pad(l)]; };
-      auto mulH = [&](int o, int l, V v) { P[pad(l)] = cmul(v, Hp[o * M + l]); };
-      fwd(cx, P, rdP, mulH);
+      auto wrP = [&](int o, int l, V v) { P[pad(l)] = v; };
+      fwd(cx, P, rdP, wrP);
+#if GNLSE_RAMAN_SPLIT
+      // spectral product and time-domain combination as separate passes over
+      // this CTA's slice (fewer live registers in the transform passes)
+      for (int l = threadIdx.x; l < M; l += T) P[pad(l)] = cmul(P[pad(l)], __ldg(&Hp[cx.rank * M + l]));
+      __syncthreads();
+      auto wrPt = [&](int o, int l, V v) { rmt(P, o)[pad(l)] = v; };
+      inv(cx, P, rdP, wrPt);
+      for (int l = threadIdx.x; l < M; l += T) {
+        const V x = X[pad(l)], conv = P[pad(l)];
+        const R p = cabs2(x);
+        X[pad(l)] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
+      }
+      __syncthreads();
+#else
+      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
       auto e3 = [&](int o, int l, V conv) {
         V* Xo = rmt(X, o);
         V x = Xo[pad(l)];
         R p = cabs2(x);
         Xo[pad(l)] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
       };
-      inv(cx, P, rdP, e3);
+      inv(cx, P, rdPH, e3);
+#endif
     }
-    double d2 = 0.0, f2 = 0.0, bad = 0.0;
-    auto rdX = [&](int o, int l) -> V { return rmt(X, o)[pad(l)]; };
-    auto fin = [&](int o, int l, V v) { stage_fin(cx, op, o * M + l, l, v, d2, f2, bad); };
-    fwd(cx, X, rdX, fin);
-    if (want_e) {
-      double s[1] = {eacc * g.dt * 1e-3};
-      cluster_sum<1>(cx, s);
-      res[0] = s[0];
-    }
-    if (op.kind == SK_S3C) {
-      double s[3] = {d2, f2, bad};
-      cluster_sum<3>(cx, s);
-      res[0] = s[0];
-      res[1] = s[1];
-      res[2] = s[2];
-    }
+    auto wrX = [&](int o, int l, V v) { X[pad(l)] = v; };
+    fwd(cx, X, rdX, wrX);
+    return energy;
   }
 
-  // Simpson energy (nJ) of G-(xhat)/N for a prologue kind SK_E_*, computed in
-  // the P buffer (X is left untouched).
-  static __device__ __noinline__ double energy_of(const Ctx& cx, const GridDev& g, const Op& op_in) {
-    const Op op = op_in;
-    const double invN2 = 1.0 / ((double)N * (double)N);
-    const int n_tot = N;
-    double eacc = 0.0;
-    auto pro = [&](int o, int l) -> V { return stage_pro(cx, op, o * M + l, l); };
-    auto ep = [&](int o, int l, V v) { eacc += simpson_w(o * M + l, n_tot) * (double)cabs2(v) * invN2; };
-    inv(cx, cx.P, pro, ep);
-    double s[1] = {eacc * g.dt * 1e-3};
+  // Simpson energy (nJ) of the time-domain powers held in buf[].x (this CTA's
+  // samples rank*M + l), summed over the cluster.
+  static __device__ double simpson_energy(const Ctx& cx, const GridDev& g, const V* buf) {
+    double e = 0.0;
+    for (int l = threadIdx.x; l < M; l += T) e += simpson_w(cx.rank * M + l, N) * (double)buf[pad(l)].x;
+    double s[1] = {e * g.dt * 1e-3};
     cluster_sum<1>(cx, s);
     return s[0];
   }
 
+  // Simpson energy (nJ) of G-(xhat)/N with xhat = pro(a, l), in the P buffer.
+  // src 0: op.MA0, 1: op.acc (global), 2: the X buffer.
+  static __device__ double energy_of(const Ctx& cx, const GridDev& g, const Op& op, int src) {
+    const R invN = (R)(1.0 / (double)N);
+    V* P = cx.P;
+    auto pl = [&](int o, int l) -> V {
+      return src == 0 ? op.MA0[o * M + l] : (src == 1 ? ldv(op.acc, o * M + l) : cx.X[pad(l)]);
+    };
+    auto ep = [&](int o, int l, V v) { rmt(P, o)[pad(l)] = mk<V>(cabs2(cscale(v, invN)), (R)0); };
+    inv(cx, P, pl, ep);
+    return simpson_energy(cx, g, P);
+  }
+
+  // ---- boundary transforms --------------------------------------------------
+  // The extended-state mode runs them in FP64, reusing the complex128
+  // transform code on the same shared memory (X and P together hold one
+  // double2 slice of M padded points).
+  using E64 = Engine<double, LOGM, C, false>;
+  static __device__ __forceinline__ typename E64::Ctx ctx64(const Ctx& cx, const GridDev& g) {
+    typename E64::Ctx c;
+    c.X = reinterpret_cast<double2*>(cx.X);
+    c.P = c.X;
+    c.red = cx.red;
+    c.tw = (const double2*)g.tw64;
+    c.twl = (const double2*)g.twl64;
+    c.rank = cx.rank;
+    return c;
+  }
+
   // time -> spectral state: S = G+(field)
-  static __device__ __noinline__ void to_spectral(const Ctx& cx, const V* field, V* S) {
-    auto pro = [&](int o, int l) -> V { return field[o * M + l]; };
-    auto epi = [&](int o, int l, V v) { S[o * M + l] = v; };
-    fwd(cx, cx.P, pro, epi);
+  static __device__ __noinline__ void to_spectral(const Ctx& cx, const GridDev& g, const FV* field, SV* S) {
+    if constexpr (XS) {
+      const typename E64::Ctx c = ctx64(cx, g);
+      auto pro = [&](int o, int l) -> double2 { return field[o * M + l]; };
+      auto epi = [&](int o, int l, double2 v) {
+        dfc_store(S, o * M + l, dfc{df_from_double(v.x), df_from_double(v.y)});
+      };
+      E64::fwd(c, c.X, pro, epi);
+    } else {
+      auto pro = [&](int o, int l) -> V { return field[o * M + l]; };
+      auto epi = [&](int o, int l, V v) { S[o * M + l] = v; };
+      fwd(cx, cx.P, pro, epi);
+    }
   }
 
   // spectral state -> time field: field = G-(S)/N
-  static __device__ __noinline__ void to_time(const Ctx& cx, const V* S, V* field) {
-    const R invN = (R)(1.0 / (double)N);
-    auto pro = [&](int o, int l) -> V { return S[o * M + l]; };
-    auto epi = [&](int o, int l, V v) { field[o * M + l] = cscale(v, invN); };
-    inv(cx, cx.P, pro, epi);
+  static __device__ __noinline__ void to_time(const Ctx& cx, const GridDev& g, const SV* S, FV* field) {
+    if constexpr (XS) {
+      const typename E64::Ctx c = ctx64(cx, g);
+      const double invN = 1.0 / (double)N;
+      auto pro = [&](int o, int l) -> double2 {
+        const dfc v = dfc_load(S, o * M + l);
+        return make_double2(df_to_double(v.re), df_to_double(v.im));
+      };
+      auto epi = [&](int o, int l, double2 v) { field[o * M + l] = make_double2(v.x * invN, v.y * invN); };
+      E64::inv(c, c.X, pro, epi);
+    } else {
+      const R invN = (R)(1.0 / (double)N);
+      auto pro = [&](int o, int l) -> V { return S[o * M + l]; };
+      auto epi = [&](int o, int l, V v) { field[o * M + l] = cscale(v, invN); };
+      inv(cx, cx.P, pro, epi);
+    }
   }
 
-  // exp(hh (i beta - alpha/2)) for this CTA's slice.  FP32 plans form the
-  // phase beta*hh in FP64 and reduce it to [-pi, pi] before the FP32 sincos.
-  static __device__ __noinline__ void exp_table(const Ctx& cx, const GridDev& g, double hh, V* Et) {
+  // exp(hh (i beta - alpha/2)) for this CTA's slice into E1; with E2 != null
+  // also E2 = exp(2 hh (i beta - alpha/2)).  The phase beta*hh is formed in
+  // FP64.  complex64 plans reduce it to [-pi, pi] before sincosf; complex128
+  // plans call sincos; extended-state plans reduce it modulo pi/512 in FP64
+  // (two-constant Cody-Waite), take cis(j pi/512) from a double-float table
+  // and cis(t), |t| <= pi/1024, from its Taylor series in double-float, and
+  // square the result for E2.
+  static __device__ __noinline__ void exp_table(const Ctx& cx, const GridDev& g, double hh, SV* E1, SV* E2) {
     const double mag = exp(-0.5 * g.alpha * hh);
-    for (int l = threadIdx.x; l < M; l += T) {
-      const int a = cx.rank * M + l;
-      double ph = g.beta[a] * hh;
-      R s, c;
-      if constexpr (sizeof(R) == 4) {
-        const double TWO_PI = 6.283185307179586476925286766559;
-        ph -= TWO_PI * rint(ph * (1.0 / TWO_PI));
-        sincosf((float)ph, &s, &c);
-      } else {
-        sincos(ph, &s, &c);
+    const int base = cx.rank * M;
+    if constexpr (XS) {
+      const float4* tab = (const float4*)g.cis_df;
+      const dff magd = df_from_double(mag);
+      const bool lossy = g.alpha != 0.0;
+      for (int l = threadIdx.x; l < M; l += T) {
+        const int a = base + l;
+        const double ph = g.beta[a] * hh;
+        const double j = rint(ph * 0x1.45f306dc9c883p+7);          // 512 / pi
+        double t = fma(-j, 0x1.921fb54000000p-8, ph);                // pi/512, high part
+        t = fma(-j, 0x1.10b4611a62633p-38, t);                       // pi/512, low part
+        const int ji = (int)(((long long)j) & 1023);
+        const dff td = df_from_double(t);
+        const float t2 = td.hi * td.hi;
+        // sin t = t - t^3/6 + t^5/120 ; cos t = 1 - t^2/2 + t^4/24
+        const dff sn = df_add_f(td, -td.hi * t2 * (1.0f / 6.0f) * (1.0f - t2 * 0.05f));
+        dff tt = two_prod(td.hi, td.hi);
+        tt.lo = fmaf(2.0f * td.hi, td.lo, tt.lo);
+        dff cs = two_sum(1.0f, -0.5f * tt.hi);
+        cs.lo += -0.5f * tt.lo + t2 * t2 * (1.0f / 24.0f);
+        cs = fast_two_sum(cs.hi, cs.lo);
+        const float4 tv = __ldg(&tab[ji]);
+        dfc e = dfc_mul(dfc{{tv.x, tv.z}, {tv.y, tv.w}}, dfc{cs, sn});
+        if (lossy) e = dfc_scale(e, magd);
+        dfc_store(E1, a, e);
+        if (E2) dfc_store(E2, a, dfc_mul(e, e));
       }
-      Et[a] = mk<V>((R)mag * c, (R)mag * s);
+    } else {
+      for (int l = threadIdx.x; l < M; l += T) {
+        const int a = base + l;
+        const double ph = g.beta[a] * hh;
+        R s, c;
+        if constexpr (sizeof(R) == 4) {
+          const double TWO_PI = 6.283185307179586476925286766559;
+          sincosf((float)(ph - TWO_PI * rint(ph * (1.0 / TWO_PI))), &s, &c);
+        } else {
+          sincos(ph, &s, &c);
+        }
+        E1[a] = mk<V>((R)mag * c, (R)mag * s);
+        if (E2) {
+          const double ph2 = g.beta[a] * (2.0 * hh);
+          const double mag2 = exp(-g.alpha * hh);
+          if constexpr (sizeof(R) == 4) {
+            const double TWO_PI = 6.283185307179586476925286766559;
+            sincosf((float)(ph2 - TWO_PI * rint(ph2 * (1.0 / TWO_PI))), &s, &c);
+          } else {
+            sincos(ph2, &s, &c);
+          }
+          E2[a] = mk<V>((R)mag2 * c, (R)mag2 * s);
+        }
+      }
     }
     __syncthreads();
   }
@@ -568,74 +621,163 @@ struct Engine {
     return (R)(g.gain_log * hh / (2.0 * g.gain_len) / (1.0 + energy / g.E_sat));
   }
 
-  // N(A) of state Z (unscaled by h) into MA, plus the gain energies of A and N(A).
-  static __device__ void state_cache(const Ctx& cx, const GridDev& g, const V* Z, V* MA,
-                                     double& eA, double& eN) {
-    Op op = {};
-    op.kind = SK_MA;
-    op.gain = g.gain;
-    op.S0 = Z;
-    op.out = MA;
-    op.MA0 = MA;
-    op.Kr = (const R*)g.Kr;
-    double res[3] = {0, 0, 0};
-    nonlinear(cx, g, op, res);
-    eA = res[0];
-    eN = 0.0;
-    if (g.gain) {
-      op.kind = SK_E_MA;
-      eN = energy_of(cx, g, op);
-    }
+  // ---- elementwise stage loops (fused end of one stage / start of the next) --
+  // X = Z (stage input of N(A) for state Z)
+  static __device__ __forceinline__ void load_state(const Ctx& cx, const SV* Z) {
+    const int base = cx.rank * M;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) cx.X[pad(l)] = ldv(Z, base + l);
+    __syncthreads();
   }
 
-  // One RK4IP evaluation of step h from state S0 (cached N(A) in MA0, gain
-  // energies eA / eN) with Et = exp(D h/2).  COARSE = false: result to out;
-  // COARSE = true: error norms against Sf in norms[0..2] and the local
-  // extrapolation of (Sf, coarse result) to out.
-  static __device__ __noinline__ void rk4ip(const Ctx& cx, const GridDev& g, const V* S0, const V* MA0,
-                                            double eA, double eN, const V* Et, V* acc, double h,
-                                            V* out, const V* Sf, bool coarse, double* norms) {
-    const double hh = 0.5 * h;
-    Op op = {};
-    op.gain = g.gain;
-    op.S0 = S0;
-    op.MA0 = MA0;
-    op.Et = Et;
-    op.acc = acc;
-    op.out = out;
-    op.Sf = Sf;
-    op.Kr = (const R*)g.Kr;
-    op.lor = (const R*)g.lor;
-    op.h = (R)h;
-    op.aA = g.gain ? gain_a(g, hh, eA) : (R)0;
-    op.ak0 = g.gain ? gain_a(g, hh, h * h * eN) : (R)0;
-    double res[3] = {0, 0, 0};
-    op.kind = SK_S1;
-    nonlinear(cx, g, op, res);
-    op.kind = SK_S2;
-    nonlinear(cx, g, op, res);
-    if (g.gain) {
-      op.kind = SK_E_ACC;
-      op.ao = gain_a(g, hh, energy_of(cx, g, op));
-      op.kind = SK_E_U;
-      op.a3 = gain_a(g, hh, energy_of(cx, g, op));
+  // MA = i K X  (N(A) of the state, unscaled by h)
+  static __device__ __forceinline__ void store_ma(const Ctx& cx, const GridDev& g, V* MA) {
+    const R* Kr = (const R*)g.Kr;
+    const int base = cx.rank * M;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) {
+      const V v = cx.X[pad(l)];
+      const R k = __ldg(&Kr[base + l]);
+      MA[base + l] = mk<V>(-k * v.y, k * v.x);
     }
-    op.kind = coarse ? SK_S3C : SK_S3;
-    nonlinear(cx, g, op, res);
+    __syncthreads();
+  }
+
+  // stage 1 input: S_I + k0/2 with S_I = L(A), k0 = L(h N(A))
+  static __device__ __forceinline__ void pre_stage1(const Ctx& cx, const Op& op) {
+    const R half = (R)0.5;
+    const int base = cx.rank * M;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const V e = ldv(op.Et, a);
+      const V si = cmul(mult(op, a, e, op.aA), ldv(op.S0, a));
+      const V k0 = cscale(cmul(mult(op, a, e, op.ak0), op.MA0[a]), op.h);
+      cx.X[pad(l)] = cadd(si, cscale(k0, half));
+    }
+    __syncthreads();
+  }
+
+  // k1 = h N; acc = S_I + k0/6 + k1/3; stage 2 input S_I + k1/2
+  static __device__ __forceinline__ void post_stage1(const Ctx& cx, const Op& op) {
+    const R half = (R)0.5, sixth = (R)(1.0 / 6.0), third = (R)(1.0 / 3.0);
+    const int base = cx.rank * M;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const V k1 = hK(op, a, cx.X[pad(l)]);
+      if constexpr (XS) {
+        const dfc e = dfc_load(op.Et, a);
+        const dfc si = dfc_mul(mult_df(op, a, e, op.aA), dfc_load(op.S0, a));
+        const V k0 = cscale(cmul(mult(op, a, dfc_hi(e), op.ak0), op.MA0[a]), op.h);
+        dfc_store(op.acc, a, dfc_add_f(si, cadd(cscale(k0, sixth), cscale(k1, third))));
+        cx.X[pad(l)] = cadd(dfc_hi(si), cscale(k1, half));
+      } else {
+        const V e = op.Et[a];
+        const V si = cmul(mult(op, a, e, op.aA), op.S0[a]);
+        const V k0 = cscale(cmul(mult(op, a, e, op.ak0), op.MA0[a]), op.h);
+        op.acc[a] = cadd(cadd(si, cscale(k0, sixth)), cscale(k1, third));
+        cx.X[pad(l)] = cadd(si, cscale(k1, half));
+      }
+    }
+    __syncthreads();
+  }
+
+  // k2 = h N; acc += k2/3; stage 3 input L(S_I + k2) (gain: S_I + k2, scaled after)
+  static __device__ __forceinline__ void post_stage2(const Ctx& cx, const Op& op) {
+    const R third = (R)(1.0 / 3.0);
+    const int base = cx.rank * M;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const V k2 = hK(op, a, cx.X[pad(l)]);
+      if constexpr (XS) {
+        dfc_store(op.acc, a, dfc_add_f(dfc_load(op.acc, a), cscale(k2, third)));
+      } else {
+        op.acc[a] = cadd(op.acc[a], cscale(k2, third));
+      }
+      const V e = ldv(op.Et, a);
+      const V u = cadd(cmul(mult(op, a, e, op.aA), ldv(op.S0, a)), k2);
+      cx.X[pad(l)] = op.gain ? u : cmul(e, u);
+    }
+    __syncthreads();
+  }
+
+  static __device__ __forceinline__ void scale_stage3(const Ctx& cx, const Op& op) {
+    const int base = cx.rank * M;
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      cx.X[pad(l)] = cmul(mult(op, a, ldv(op.Et, a), op.a3), cx.X[pad(l)]);
+    }
+    __syncthreads();
+  }
+
+  // k3 = h N; result = L(acc) + k3/6 -> out; coarse: error norms against Sf and
+  // the local extrapolation (stepper.py:272-274,338) (16 A_fine - A_coarse)/15 -> out.
+  static __device__ __forceinline__ void post_stage3(const Ctx& cx, const Op& op, bool coarse,
+                                                     double (&s)[3]) {
+    const R sixth = (R)(1.0 / 6.0);
+    const R fa = (R)(16.0 / 15.0), fb = (R)(1.0 / 15.0);
+    const int base = cx.rank * M;
+    R d2 = 0, f2 = 0;
+    double bad = 0.0;
+#pragma unroll 4
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const V k3 = hK(op, a, cx.X[pad(l)]);
+      if constexpr (XS) {
+        const dfc res = dfc_add_f(dfc_mul(mult_df(op, a, dfc_load(op.Et, a), op.ao), dfc_load(op.acc, a)),
+                                  cscale(k3, sixth));
+        if (!coarse) {
+          dfc_store(op.out, a, res);
+        } else {
+          const dfc sf = dfc_load(op.Sf, a);
+          const dfc d = dfc_sub(sf, res);
+          d2 += d.re.hi * d.re.hi + d.im.hi * d.im.hi;
+          f2 += sf.re.hi * sf.re.hi + sf.im.hi * sf.im.hi;
+          if (!isfinite(sf.re.hi) || !isfinite(sf.im.hi)) bad = 1.0;
+          const dff FA = {(float)(16.0 / 15.0), (float)(16.0 / 15.0 - (double)(float)(16.0 / 15.0))};
+          const dff FB = {(float)(-1.0 / 15.0), (float)(-1.0 / 15.0 - (double)(float)(-1.0 / 15.0))};
+          dfc_store(op.out, a, dfc_add(dfc_scale(sf, FA), dfc_scale(res, FB)));
+        }
+      } else {
+        const V res = cadd(cmul(mult(op, a, op.Et[a], op.ao), op.acc[a]), cscale(k3, sixth));
+        if (!coarse) {
+          op.out[a] = res;
+        } else {
+          const V sf = op.Sf[a];
+          const V d = csub(sf, res);
+          d2 += cabs2(d);
+          f2 += cabs2(sf);
+          if (!isfinite(sf.x) || !isfinite(sf.y)) bad = 1.0;
+          op.out[a] = mk<V>(fa * sf.x - fb * res.x, fa * sf.y - fb * res.y);
+        }
+      }
+    }
+    s[0] = d2;
+    s[1] = f2;
+    s[2] = bad;
     if (coarse) {
-      norms[0] = res[0];
-      norms[1] = res[1];
-      norms[2] = res[2];
+      cluster_sum<3>(cx, s);
+    } else {
+      __syncthreads();
     }
   }
 
   // FP64 energy (Parseval, nJ) and photon number of state S.
-  static __device__ __noinline__ void diagnostics(const Ctx& cx, const GridDev& g, const V* S,
+  static __device__ __noinline__ void diagnostics(const Ctx& cx, const GridDev& g, const SV* S,
                                                   double* E, double* Nph) {
     double e = 0.0, p = 0.0;
     for (int l = threadIdx.x; l < M; l += T) {
       const int a = cx.rank * M + l;
-      const double s2 = (double)cabs2(S[a]);
+      double s2;
+      if constexpr (XS) {
+        const dfc v = dfc_load(S, a);
+        const double re = df_to_double(v.re), im = df_to_double(v.im);
+        s2 = re * re + im * im;
+      } else {
+        s2 = (double)cabs2(S[a]);
+      }
       e += s2;
       p += s2 / g.nu[a];
     }
@@ -646,21 +788,39 @@ struct Engine {
     *Nph = s[1] * scale / 6.62607015e-10;
   }
 
-  static __device__ void store_trace(const Ctx& cx, const KParams& kp, const InstDev& d,
-                                     InstState& st, const V* S, double z) {
-    if (st.ntraces >= d.max_traces) {
-      st.trace_overflow = 1;
+  // Per-CTA control block in shared memory: uniform state read by all
+  // threads, written by thread 0 between barriers.
+  struct Ctl {
+    GridDev g;
+    InstDev d;
+    InstState st;
+    Op op;
+    double eA[2], eN[2];
+  };
+  static_assert(sizeof(Ctl) <= 1024, "control block size");
+
+  static __device__ void store_trace(const Ctx& cx, const KParams& kp, Ctl& c, const SV* S, double z) {
+    if (c.st.ntraces >= c.d.max_traces) {
+      __syncthreads();
+      if (threadIdx.x == 0) c.st.trace_overflow = 1;
+      __syncthreads();
       return;
     }
-    V* tr = (V*)kp.traces + d.trace_off + (long long)st.ntraces * N;
-    to_time(cx, S, tr);
-    if (cx.rank == 0 && threadIdx.x == 0) kp.trace_z[d.tracez_off + st.ntraces] = z;
-    st.ntraces += 1;
+    FV* tr = (FV*)kp.traces + c.d.trace_off + (long long)c.st.ntraces * N;
+    to_time(cx, c.g, S, tr);
+    if (cx.rank == 0 && threadIdx.x == 0) kp.trace_z[c.d.tracez_off + c.st.ntraces] = z;
+    __syncthreads();
+    if (threadIdx.x == 0) c.st.ntraces += 1;
+    __syncthreads();
   }
 
-  // The whole propagation of one instance.  Control state lives in shared
-  // memory; every thread evaluates the same decisions from the same
-  // cluster-reduced values, so all CTAs of a cluster follow one path.
+  // The whole propagation of one instance.  Every CTA of a cluster evaluates
+  // the same control decisions from the same cluster-reduced values, so all
+  // CTAs follow one path.  An attempt is a loop over its nonlinear
+  // evaluations ("slots"), so the transform code is inlined once:
+  //   adaptive: N(A) of S, 3 stages of rk4ip(S, h/2) -> Sh, N(A) of Sh,
+  //             3 stages of rk4ip(Sh, h/2) -> Sf, 3 stages of rk4ip(S, h) -> Sh'
+  //   fixed   : N(A) of S, 3 stages of rk4ip(S, h) -> S'
   static __device__ void run(const KParams& kp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cid = blockIdx.x / C;
@@ -669,10 +829,7 @@ struct Engine {
     cx.X = (V*)smem_raw;
     cx.P = cx.X + MP;
     cx.red = (double*)(cx.P + MP);
-    unsigned char* ctl = (unsigned char*)(cx.red + RED);
-    GridDev& g = *(GridDev*)ctl;
-    InstDev& d = *(InstDev*)(ctl + 192);
-    static_assert(sizeof(GridDev) <= 192 && sizeof(InstDev) <= 128, "control block layout");
+    Ctl& c = *(Ctl*)(cx.red + RED);
     if constexpr (C > 1) {
       cx.rank = (int)cg::this_cluster().block_rank();
     } else {
@@ -680,138 +837,205 @@ struct Engine {
     }
     const int id = kp.order[cid];
     if (threadIdx.x == 0) {
-      d = kp.inst[id];
-      g = kp.grids[d.grid];
+      c.d = kp.inst[id];
+      c.g = kp.grids[c.d.grid];
+      c.st = kp.state[id];
+      c.eA[0] = c.st.cache_eA;
+      c.eN[0] = c.st.cache_eN;
+      c.eA[1] = c.eN[1] = 0.0;
     }
     __syncthreads();
+    const GridDev& g = c.g;
+    const InstDev& d = c.d;
+    InstState& st = c.st;
+    Op& op = c.op;
     cx.tw = (const V*)g.tw;
-    InstState st = kp.state[id];
-    V* field = (V*)kp.fields + d.field_off;
-    V* base = (V*)kp.scratch + d.scratch_off;
-    V* Sbuf[2] = {base, base + N};
-    V* Sf = base + 2 * N;
-    V* MA = base + 3 * N;
-    V* MAh = base + 4 * N;
-    V* acc = base + 5 * N;
-    V* E1 = base + 6 * N;
-    V* E2 = base + 7 * N;
+    cx.twl = (const V*)g.twl;
+    FV* field = (FV*)kp.fields + d.field_off;
+    SV* base = (SV*)kp.scratch + d.scratch_off;
     long long budget = kp.max_attempts > 0 ? kp.max_attempts : (1ll << 62);
 
     if (st.phase == 0) {
-      st.ntraces = 0;
-      st.trace_overflow = 0;
+      int ntr = 0, ovf = 0;
       if (d.method == 1 && d.traces != 1) {
         if (d.max_traces > 0) {
-          V* tr = (V*)kp.traces + d.trace_off;
+          FV* tr = (FV*)kp.traces + d.trace_off;
           for (int l = threadIdx.x; l < M; l += T) tr[cx.rank * M + l] = field[cx.rank * M + l];
           if (cx.rank == 0 && threadIdx.x == 0) kp.trace_z[d.tracez_off] = 0.0;
-          st.ntraces = 1;
+          ntr = 1;
         } else {
-          st.trace_overflow = 1;
+          ovf = 1;
         }
       }
-      to_spectral(cx, field, Sbuf[0]);
-      diagnostics(cx, g, Sbuf[0], &st.E_in, &st.Nph_in);
-      st.sidx = 0;
-      st.z = 0.0;
-      st.h = d.method == 1 ? d.h0 : d.length / d.total_steps;
-      st.z_ignore = d.length / d.traces;
-      st.ma_valid = 0;
-      st.ta = 0;
-      st.status = ST_RUNNING;
-      st.phase = 1;
+      to_spectral(cx, g, field, base);
+      double e_in, n_in;
+      diagnostics(cx, g, base, &e_in, &n_in);
+      if (threadIdx.x == 0) {
+        st.ntraces = ntr;
+        st.trace_overflow = ovf;
+        st.E_in = e_in;
+        st.Nph_in = n_in;
+        st.sidx = 0;
+        st.z = 0.0;
+        st.h = d.method == 1 ? d.h0 : d.length / d.total_steps;
+        st.z_ignore = d.length / d.traces;
+        st.ma_valid = 0;
+        st.ta = 0;
+        st.status = ST_RUNNING;
+        st.phase = 1;
+      }
+      __syncthreads();
     }
 
-    if (st.phase == 1 && d.method == 0) {
-      // Fixed-step driver (stepper.py:164-221); exp(D h/2) is computed once,
-      // as Linearity.default_exp_f_cached does (linearity.py:258-262).
-      const double h = d.length / d.total_steps;
-      const double dz = d.length / d.total_steps;  // numpy linspace step of the z mesh
-      const int storage_step = d.traces > 0 ? d.total_steps / d.traces : 0;
-      exp_table(cx, g, 0.5 * h, E2);
-      while (st.steps < d.total_steps && budget > 0) {
-        V* S = Sbuf[st.sidx];
-        V* Sn = Sbuf[st.sidx ^ 1];
-        double eA = 0, eN = 0;
-        state_cache(cx, g, S, MA, eA, eN);
-        rk4ip(cx, g, S, MA, eA, eN, E2, acc, h, Sn, nullptr, false, nullptr);
-        st.sidx ^= 1;
-        st.evals += 1;
-        st.attempts += 1;
-        st.accepted += 1;
-        budget -= 1;
-        const long long i = st.steps;
-        st.steps += 1;
-        st.z = (st.steps == d.total_steps) ? d.length : (double)st.steps * dz;
-        if (d.traces != 1 && storage_step > 0 && (i % storage_step) == 0)
-          store_trace(cx, kp, d, st, Sbuf[st.sidx], (double)i * dz + h);
-      }
-      if (st.steps >= d.total_steps) {
-        st.status = ST_OK;
-        st.phase = 2;
-      }
-    }
+    const bool adaptive = d.method == 1;
+    if (st.phase == 1 && !adaptive) exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
 
-    if (st.phase == 1 && d.method == 1) {
-      // Adaptive driver (stepper.py:247-376): step doubling, eta = 5.
-      const double tol = d.tol;
-      const double step_storage = d.length / d.traces;
-      while (st.phase == 1 && budget > 0) {
-        if (st.ta == 0) {
-          if (st.steps >= 99999) {  // for s in range(1, steps_max)
-            st.status = ST_MAX_STEPS;
-            st.phase = 2;
-            break;
+    while (st.phase == 1 && budget > 0) {
+      // ---- one attempt (adaptive) or one step (fixed) ------------------------
+      if (threadIdx.x == 0) {
+        if (adaptive) {
+          if (st.ta == 0) {
+            if (st.steps >= 99999) {  // for s in range(1, steps_max) (stepper.py:289)
+              st.status = ST_MAX_STEPS;
+              st.phase = 2;
+            } else if (st.z + st.h > d.length) {
+              st.h = d.length - st.z;
+            }
           }
-          if (st.z + st.h > d.length) st.h = d.length - st.z;
+        } else {
+          st.ma_valid = 0;
         }
-        V* S = Sbuf[st.sidx];
-        V* Sh = Sbuf[st.sidx ^ 1];
-        if (!st.ma_valid) {
-          state_cache(cx, g, S, MA, st.cache_eA, st.cache_eN);
-          st.ma_valid = 1;
+      }
+      __syncthreads();
+      if (st.phase != 1) break;
+      const double h = adaptive ? st.h : d.length / d.total_steps;
+      const int sidx = st.sidx;
+      if (adaptive) exp_table(cx, g, 0.25 * h, base + 6 * N, base + 7 * N);
+      const int q_end = adaptive ? 11 : 4;
+      double nrm[3] = {0.0, 0.0, 0.0};
+      for (int q = st.ma_valid ? 1 : 0; q < q_end; ++q) {
+        // slot q: kind 0 = N(A) of state mi, kind 1..3 = stage of evaluation e
+        const int kind = (q == 0 || q == 4) ? 0 : (q < 4 ? q : (q < 8 ? q - 4 : q - 7));
+        const int mi = q == 4 ? 1 : 0;
+        SV* S = base + (long long)sidx * N;
+        SV* Sh = base + (long long)(sidx ^ 1) * N;
+        if (kind == 1) {
+          if (threadIdx.x == 0) {
+            const int e = q < 4 ? 0 : (q < 8 ? 1 : 2);
+            const double he = (adaptive && e < 2) ? 0.5 * h : h;
+            const int m = e == 1 ? 1 : 0;
+            op.Kr = (const R*)g.Kr;
+            op.lor = (const R*)g.lor;
+            op.gain = g.gain;
+            op.acc = base + 5 * N;
+            op.Sf = base + 2 * N;
+            op.S0 = e == 1 ? Sh : S;
+            op.MA0 = reinterpret_cast<V*>(base + (3 + m) * N);
+            op.Et = base + ((adaptive && e < 2) ? 6 : 7) * N;
+            op.out = e == 1 ? base + 2 * N : Sh;
+            op.h = (R)he;
+            op.hh = 0.5 * he;
+            op.aA = g.gain ? gain_a(g, 0.5 * he, c.eA[m]) : (R)0;
+            op.ak0 = g.gain ? gain_a(g, 0.5 * he, he * he * c.eN[m]) : (R)0;
+            op.a3 = op.ao = (R)0;
+          }
+          __syncthreads();
+          pre_stage1(cx, op);
+        } else if (kind == 0) {
+          load_state(cx, mi == 0 ? S : Sh);
         }
-        const double h = st.h;
-        const double h_half = 0.5 * h;
-        exp_table(cx, g, 0.5 * h_half, E1);
-        exp_table(cx, g, 0.5 * h, E2);
-        rk4ip(cx, g, S, MA, st.cache_eA, st.cache_eN, E1, acc, h_half, Sh, nullptr, false, nullptr);
-        double eAh = 0, eNh = 0;
-        state_cache(cx, g, Sh, MAh, eAh, eNh);
-        rk4ip(cx, g, Sh, MAh, eAh, eNh, E1, acc, h_half, Sf, nullptr, false, nullptr);
-        double nrm[3];
-        rk4ip(cx, g, S, MA, st.cache_eA, st.cache_eN, E2, acc, h, Sh, Sf, true, nrm);
-        st.evals += 3;
+        const double en = nonlinear(cx, g, kind == 0 && g.gain);
+        if (kind == 0) {
+          V* MA = reinterpret_cast<V*>(base + (3 + mi) * N);
+          store_ma(cx, g, MA);
+          double eN = 0.0;
+          if (g.gain) {
+            if (threadIdx.x == 0) op.MA0 = MA;
+            __syncthreads();
+            eN = energy_of(cx, g, op, 0);
+          }
+          if (threadIdx.x == 0) {
+            c.eA[mi] = en;
+            c.eN[mi] = eN;
+            if (mi == 0) {
+              st.ma_valid = 1;
+              st.cache_eA = en;
+              st.cache_eN = eN;
+            }
+          }
+          __syncthreads();
+        } else if (kind == 1) {
+          post_stage1(cx, op);
+        } else if (kind == 2) {
+          post_stage2(cx, op);
+          if (g.gain) {
+            const double e_acc = energy_of(cx, g, op, 1);
+            const double e_u = energy_of(cx, g, op, 2);
+            if (threadIdx.x == 0) {
+              op.ao = gain_a(g, op.hh, e_acc);
+              op.a3 = gain_a(g, op.hh, e_u);
+            }
+            __syncthreads();
+            scale_stage3(cx, op);
+          }
+        } else {
+          post_stage3(cx, op, adaptive && q == 10, nrm);
+          if (threadIdx.x == 0) st.evals += 1;
+        }
+      }
+      budget -= 1;
+
+      if (!adaptive) {
+        // Fixed-step driver (stepper.py:164-221)
+        const double dz = d.length / d.total_steps;  // numpy linspace step of the z mesh
+        const int storage_step = d.traces > 0 ? d.total_steps / d.traces : 0;
+        const long long i = st.steps;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          st.attempts += 1;
+          st.sidx ^= 1;
+          st.accepted += 1;
+          st.steps += 1;
+          st.z = (st.steps == d.total_steps) ? d.length : (double)st.steps * dz;
+          if (st.steps >= d.total_steps) {
+            st.status = ST_OK;
+            st.phase = 2;
+          }
+        }
+        __syncthreads();
+        if (d.traces != 1 && storage_step > 0 && (i % storage_step) == 0)
+          store_trace(cx, kp, c, base + (long long)st.sidx * N, (double)i * dz + h);
+        continue;
+      }
+
+      // Adaptive driver (stepper.py:247-376); relative_local_error (stepper.py:231-245)
+      double delta;
+      if (nrm[2] != 0.0 || !isfinite(nrm[1])) {
+        delta = 1.0;
+      } else {
+        const double nf = sqrt(nrm[1]);
+        delta = nf != 0.0 ? sqrt(nrm[0]) / nf : sqrt(nrm[0]);
+      }
+      const bool accept = delta < 2.0 * d.tol;
+      __syncthreads();
+      if (threadIdx.x == 0) {
         st.attempts += 1;
         st.ta += 1;
-        budget -= 1;
-        // relative_local_error (stepper.py:231-245)
-        double delta;
-        if (nrm[2] != 0.0 || !isfinite(nrm[1])) {
-          delta = 1.0;
-        } else {
-          const double nf = sqrt(nrm[1]);
-          delta = nf != 0.0 ? sqrt(nrm[0]) / nf : sqrt(nrm[0]);
-        }
         st.delta_last = delta;
         const double h_temp = h;
         if (delta > 0.0) {
-          const double factor = 0.9 * pow(tol / delta, 1.0 / 5.0);
+          const double factor = 0.9 * pow(d.tol / delta, 1.0 / 5.0);
           st.h = h_temp * fmin(10.0, fmax(0.2, factor));
         } else {
           st.h = h_temp * 10.0;
         }
-        if (delta < 2.0 * tol) {
+        if (accept) {
           st.z += h_temp;
-          st.sidx ^= 1;  // Sh now holds the extrapolated solution
+          st.sidx ^= 1;  // Sh holds the extrapolated solution
           st.ma_valid = 0;
           st.accepted += 1;
           st.steps += 1;
           st.ta = 0;
-          if (st.z > st.z_ignore) {
-            store_trace(cx, kp, d, st, Sbuf[st.sidx], st.z);
-            st.z_ignore += step_storage;
-          }
           if (st.z >= d.length) {
             st.status = ST_OK;
             st.phase = 2;
@@ -827,29 +1051,42 @@ struct Engine {
           }
         }
       }
+      __syncthreads();
+      if (accept && st.z > st.z_ignore) {
+        store_trace(cx, kp, c, base + (long long)st.sidx * N, st.z);
+        if (threadIdx.x == 0) st.z_ignore += d.length / d.traces;
+        __syncthreads();
+      }
     }
 
     if (st.phase == 2) {
-      to_time(cx, Sbuf[st.sidx], field);
-      diagnostics(cx, g, Sbuf[st.sidx], &st.E_out, &st.Nph_out);
-      st.phase = 3;
+      const SV* S = base + (long long)st.sidx * N;
+      to_time(cx, g, S, field);
+      double e_out, n_out;
+      diagnostics(cx, g, S, &e_out, &n_out);
+      if (threadIdx.x == 0) {
+        st.E_out = e_out;
+        st.Nph_out = n_out;
+        st.phase = 3;
+      }
     }
     __syncthreads();
     if (cx.rank == 0 && threadIdx.x == 0) kp.state[id] = st;
   }
 };
 
-template <class R, int LOGM, int C>
-__global__ void __launch_bounds__(Engine<R, LOGM, C>::T) gnlse_kernel(KParams kp) {
-  Engine<R, LOGM, C>::run(kp);
+template <class R, int LOGM, int C, bool XS>
+__global__ void __launch_bounds__(Engine<R, LOGM, C, XS>::T, Engine<R, LOGM, C, XS>::MINB)
+    gnlse_kernel(KParams kp) {
+  Engine<R, LOGM, C, XS>::run(kp);
 }
 
 // Host launcher for one (precision, M, C) class: one cluster per instance.
-template <class R, int LOGM, int C>
+template <class R, int LOGM, int C, bool XS>
 cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream) {
-  using E = Engine<R, LOGM, C>;
+  using E = Engine<R, LOGM, C, XS>;
   const size_t smem = E::smem_bytes();
-  cudaError_t err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C>,
+  cudaError_t err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C, XS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   cudaLaunchConfig_t cfg = {};
@@ -868,7 +1105,7 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
   }
   cfg.attrs = attr;
   cfg.numAttrs = na;
-  return cudaLaunchKernelEx(&cfg, gnlse_kernel<R, LOGM, C>, kp);
+  return cudaLaunchKernelEx(&cfg, gnlse_kernel<R, LOGM, C, XS>, kp);
 }
 
 }  // namespace gnlse

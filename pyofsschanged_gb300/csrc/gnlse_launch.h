@@ -7,20 +7,28 @@
 
 namespace gnlse {
 
-template <class R, int LOGM, int C>
+template <class R, int LOGM, int C, bool XS>
 cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream);
 
-template <class R, int LOGM, int C>
-size_t class_smem_bytes();
-
 // (precision, log2 M, C) classes compiled into the library.
+#ifdef GNLSE_ENSEMBLE_SUBSET
+// tuning builds: only the FP32 classes of the ensemble benchmark
+#define GNLSE_CLASSES_F32(X) X(float, 12, 1) X(float, 12, 2) X(float, 12, 4) X(float, 13, 1) X(float, 13, 2)
+#define GNLSE_CLASSES_F64(X)
+#define GNLSE_CLASSES_MIX(X) X(float, 12, 1) X(float, 12, 2) X(float, 12, 4)
+#else
 #define GNLSE_CLASSES_F32(X) \
   X(float, 8, 1) X(float, 9, 1) X(float, 10, 1) X(float, 11, 1) X(float, 12, 1) X(float, 13, 1) \
   X(float, 8, 2) X(float, 9, 2) X(float, 10, 2) X(float, 12, 2) X(float, 13, 2) \
-  X(float, 8, 4) X(float, 12, 4) X(float, 13, 4) X(float, 13, 8)
+  X(float, 8, 4) X(float, 12, 4) X(float, 13, 4) X(float, 12, 8) X(float, 13, 8)
 #define GNLSE_CLASSES_F64(X) \
   X(double, 8, 1) X(double, 9, 1) X(double, 10, 1) X(double, 11, 1) X(double, 12, 1) \
   X(double, 8, 2) X(double, 9, 2) X(double, 10, 2) X(double, 11, 2) X(double, 12, 2) \
   X(double, 8, 4) X(double, 12, 4) X(double, 12, 8)
+// extended-state (mixed precision) classes: complex64 transforms
+#define GNLSE_CLASSES_MIX(X) \
+  X(float, 8, 1) X(float, 9, 1) X(float, 10, 1) X(float, 11, 1) X(float, 12, 1) \
+  X(float, 9, 2) X(float, 12, 2) X(float, 8, 4) X(float, 12, 4) X(float, 12, 8) X(float, 13, 8)
+#endif
 
 }  // namespace gnlse

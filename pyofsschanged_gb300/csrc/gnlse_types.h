@@ -15,7 +15,11 @@ struct GridDev {
   const void* Hp;       // [N] complex: fft(h_R) * window_t / N   (null: no Raman)
   const void* lor;      // [N] real: gain profile                   (null: no gain)
   const double* nu;     // [N] absolute frequency (THz), FP64, for photon number
-  const void* tw;       // [N] natural order: exp(+2 pi i j / N)
+  const void* tw;       // [N] natural order: exp(+2 pi i j / N) (cross-CTA pass)
+  const void* twl;      // [M] natural order: exp(+2 pi i j / M) (per-CTA transform)
+  const void* tw64;     // extended-state plans: FP64 copies of tw and twl
+  const void* twl64;
+  const void* cis_df;   // extended-state plans: [1024] double-float cis(j pi / 512)
   int n, logm, C, raman;
   int gain, pad0;
   double alpha;         // 1/km, linear attenuation

@@ -3,7 +3,8 @@
 A :class:`Plan` owns the device operator tables, per-instance state and
 scratch of the C engine (include/gnlse.h).  Fields are torch tensors on the
 current CUDA device: complex64 for ``precision="fp32"``, complex128 for
-``"fp64"``, concatenated per instance in the order given.
+``"fp64"`` and ``"mixed"`` (complex64 transforms with a double-float state),
+concatenated per instance in the order given.
 """
 
 import ctypes as ct
@@ -13,7 +14,7 @@ import torch
 
 from . import _native as nat
 
-PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64}
+PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE_MIXED}
 METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP}
 
 
@@ -51,7 +52,7 @@ class Instance:
 class Plan:
     def __init__(self, grids, instances, precision="fp32", device=None):
         if precision not in PRECISIONS:
-            raise ValueError("precision must be 'fp32' or 'fp64'")
+            raise ValueError("precision must be 'fp32', 'mixed' or 'fp64'")
         lib = nat.lib()
         self.precision = precision
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
@@ -166,6 +167,19 @@ class Plan:
                                                  ct.c_void_p(s.cuda_stream)),
                   "gnlse_propagate_host")
         return hout
+
+    def set_timing(self, enable=True):
+        nat.check(nat.lib().gnlse_set_timing(self.handle, 1 if enable else 0), "gnlse_set_timing")
+
+    def class_times(self):
+        """[(log2 points per CTA, cluster size, instances, kernel ms)] of the last propagate."""
+        k = 16
+        lm, cl, cnt = (ct.c_int32 * k)(), (ct.c_int32 * k)(), (ct.c_int32 * k)()
+        ms = (ct.c_double * k)()
+        nc = nat.lib().gnlse_class_times(self.handle, k, lm, cl, cnt, ms)
+        if nc < 0:
+            raise nat.GnlseError(-nc, "gnlse_class_times")
+        return [(lm[i], cl[i], cnt[i], ms[i]) for i in range(nc)]
 
     def stats(self, stream=None):
         s = stream or torch.cuda.current_stream(self.device)

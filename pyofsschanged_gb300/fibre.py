@@ -6,8 +6,9 @@ propagates the field through the fibre and returns it, as
 ``Fibre.__call__`` does (fibre.py:136-148).  ``method`` selects the engine
 path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps) or
 ``"cuda_ark4ip"`` / ``"ark4ip"`` (adaptive step doubling with tolerance
-``local_error``).  ``precision`` selects complex64 (``"fp32"``, default) or
-complex128 (``"fp64"``) propagation.  The stepper exceptions of
+``local_error``).  ``precision`` selects ``"mixed"`` (default: complex64
+transforms with a double-float propagation state), ``"fp32"`` (complex64
+throughout) or ``"fp64"`` (complex128 throughout).  The stepper exceptions of
 pyofss/modules/stepper.py:33-47 are raised with the same names.
 
 Models outside the CUDA path (WDM two-channel, the legacy ``raman_scattering``
@@ -91,7 +92,7 @@ class Fibre:
                  small_signal_gain=None, E_sat=None, P_sat=None, Tr=None, lamb0=None,
                  bandwidth=None, use_Er_profile=False, use_Er_noise=False, use_Yb_model=False,
                  Pp_0=None, N=None, Rr=None, dir=None, save_represent="power", cycle=None,
-                 downsampling=None, precision="fp32", cluster=0):
+                 downsampling=None, precision="mixed", cluster=0):
         m = method.lower()
         if m.startswith("cuda_"):
             m = m[5:]

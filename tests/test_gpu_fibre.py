@@ -1,0 +1,44 @@
+"""The drop-in module path: System + Sech + Fibre(method='cuda_ark4ip'/'cuda_rk4ip')."""
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from oracle import gnlse_oracle as go
+from pyofsschanged_gb300 import (Domain, Fibre, Gaussian, Sech, SmallStepSizeError, System)
+
+pytestmark = pytest.mark.gpu
+
+
+def spec_err(a, b):
+    return float(np.linalg.norm(go.fft(a) - go.fft(b)) / np.linalg.norm(go.fft(b)))
+
+
+@pytest.mark.parametrize("name,precision,tol", [
+    ("sc_blowwood_ark4ip_1024", "fp64", 1e-9), ("sc_blowwood_ark4ip_1024", "mixed", 1e-4),
+    ("gain_ark4ip_1024", "mixed", 1e-4), ("soliton_n2_1024", "fp64", 1e-9)])
+def test_system_with_cuda_fibre(cuda_ready, name, precision, tol):
+    case = gc.load(name)
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    p = dict(prm["pulse"])
+    cls = Sech if p.pop("kind") == "sech" else Gaussian
+    fk = gc.fibre_kwargs(prm)
+    fk["method"] = "cuda_" + fk["method"]
+    sys_ = System(d)
+    sys_.add(cls(**p))
+    sys_.add(Fibre(precision=precision, **fk))
+    sys_.run()
+    out = sys_.fields["fibre"]
+    assert spec_err(out, case["A_out"]) <= tol
+    st = sys_["fibre"].stepper
+    np.testing.assert_allclose(st.storage.z, case["trace_z"], rtol=1e-9)
+
+
+def test_fibre_raises_reference_exception(cuda_ready):
+    d = Domain(bit_width=12.5, samples_per_bit=1024, centre_nu=359.0)
+    a = Sech(peak_power=100.0, width=0.1)(d, np.zeros(1024, complex))
+    a[5] = np.inf
+    fib = Fibre(length=1e-5, beta=[0, 0, -10.0], gamma=100.0, method="cuda_ark4ip")
+    with pytest.raises(SmallStepSizeError):
+        fib(d, a)
