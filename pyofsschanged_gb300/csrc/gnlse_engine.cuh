@@ -33,6 +33,14 @@
 #ifndef GNLSE_RAMAN_SPLIT
 #define GNLSE_RAMAN_SPLIT 0
 #endif
+// log2 of the radix of the Stockham passes (3: radix 8, 4: radix 16) and the
+// points each thread holds per pass
+#ifndef GNLSE_RADIX_BITS
+#define GNLSE_RADIX_BITS 4
+#endif
+#ifndef GNLSE_PPT
+#define GNLSE_PPT 16
+#endif
 
 namespace cg = cooperative_groups;
 
@@ -126,7 +134,9 @@ __device__ __forceinline__ double simpson_w(int n, int N) {
 // XS ("extended state"): complex64 transforms and nonlinear evaluations with
 // the propagation state, the RK accumulator and the exp(hD) factors held as
 // double-float complex values (float4) and FP64 boundary transforms.
-template <class R, int LOGM, int C, bool XS = false>
+// INPLACE: cross-CTA passes exchange in place (no exchange buffer); used for
+// the FP64 boundary transforms of extended-state kernels.
+template <class R, int LOGM, int C, bool XS = false, bool INPLACE = false>
 struct Engine {
   using V = typename VT<R>::V;
   using SV = typename std::conditional<XS, float4, V>::type;  // state-like arrays
@@ -134,27 +144,31 @@ struct Engine {
   static_assert(!XS || sizeof(R) == 4, "extended state runs on complex64 transforms");
   static constexpr int M = 1 << LOGM;
   static constexpr int N = M * C;
-  static constexpr int T = (M / 16) < 64 ? 64 : (M / 16);
+  static constexpr int T = (M / GNLSE_PPT) < 64 ? 64 : (M / GNLSE_PPT);
   static constexpr int MP = M + M / 16;
-  static constexpr int NR16 = LOGM / 4;
-  static constexpr int REM = LOGM % 4;
+  static constexpr int RB = GNLSE_RADIX_BITS;  // log2 of the main radix
+  static constexpr int RADIX = 1 << RB;
+  static constexpr int NR16 = LOGM / RB;        // passes of the main radix
+  static constexpr int REM = LOGM % RB;         // log2 of the final smaller radix
   static constexpr int RED = 64;  // doubles of reduction scratch
   static_assert(LOGM >= 8, "M >= 256 required");
   static_assert(C == 1 || C == 2 || C == 4 || C == 8, "cluster size 1, 2, 4 or 8");
   static constexpr size_t ctl_bytes() { return 1024; }
   // CTAs that fit on one SM by shared memory (228 KB per SM, 1 KB reserved per CTA)
-  static constexpr int MINB_RAW = (int)(233472 / (2 * MP * sizeof(V) + RED * sizeof(double) + 1024 + 1024));
+  static constexpr int NBUF = (C > 1 && !INPLACE) ? 3 : 2;  // X, P (+ W)
+  static constexpr int MINB_RAW = (int)(233472 / (NBUF * MP * sizeof(V) + RED * sizeof(double) + 1024 + 1024));
   // ... capped so that a thread keeps at least 64 registers (and at most
   // GNLSE_MINB_CAP CTAs per SM are assumed when allocating registers)
   static constexpr int MINB_REG = MINB_RAW < 1 ? 1 : (MINB_RAW * T > 1024 ? 1024 / T : MINB_RAW);
   static constexpr int MINB = MINB_REG < GNLSE_MINB_CAP ? MINB_REG : GNLSE_MINB_CAP;
   static constexpr size_t smem_bytes() {
-    return 2 * MP * sizeof(V) + RED * sizeof(double) + ctl_bytes();
+    return NBUF * MP * sizeof(V) + RED * sizeof(double) + ctl_bytes();
   }
 
   struct Ctx {
     V* X;
     V* P;
+    V* W;          // exchange buffer of the cross-CTA passes (C > 1)
     double* red;
     const V* tw;   // N-point table (cross-CTA pass)
     const V* twl;  // M-point table (per-CTA passes)
@@ -184,11 +198,12 @@ struct Engine {
   }
 
   // ---- transforms ---------------------------------------------------------
-  // One in-place radix-RAD Stockham pass over the CTA's M points (all loads,
-  // barrier, all stores).  FIRST: inputs from pro(owner, slot); LAST: outputs
-  // to epi(owner, slot, v); otherwise the padded shared buffer.
+  // One radix-RAD Stockham pass over the CTA's M points: all loads, barrier,
+  // all stores (so src may equal dst).  FIRST: inputs from pro(owner, slot),
+  // otherwise from src; LAST: outputs to epi(owner, slot, v), otherwise to dst.
   template <int RAD, int SIGN, bool FIRST, bool LAST, class Pro, class Epi>
-  static __device__ __forceinline__ void pass(const Ctx& cx, V* buf, int Ns, Pro& pro, Epi& epi) {
+  static __device__ __forceinline__ void pass(const Ctx& cx, const V* src, V* dst, int Ns, Pro& pro,
+                                              Epi& epi) {
     constexpr int NB = M / RAD;
     constexpr int BPT = (NB + T - 1) / T;
     V v[BPT][RAD];
@@ -201,7 +216,7 @@ struct Engine {
         for (int r = 0; r < RAD; ++r) {
           const int i = j + r * NB;
           if constexpr (FIRST) v[b][r] = pro(cx.rank, i);
-          else v[b][r] = buf[pad(i)];
+          else v[b][r] = src[pad(i)];
         }
       }
     }
@@ -222,7 +237,7 @@ struct Engine {
         for (int r = 0; r < RAD; ++r) {
           const int o = base + r * Ns;
           if constexpr (LAST) epi(cx.rank, o, v[b][r]);
-          else buf[pad(o)] = v[b][r];
+          else dst[pad(o)] = v[b][r];
         }
       }
     }
@@ -230,99 +245,134 @@ struct Engine {
   }
 
   template <int SIGN, bool PRO, bool EPI, int P16, class Pro, class Epi>
-  static __device__ __forceinline__ void passes16(const Ctx& cx, V* buf, int Ns, Pro& pro, Epi& epi) {
+  static __device__ __forceinline__ void passes(const Ctx& cx, const V* src, V* buf, V* dst, int Ns,
+                                                Pro& pro, Epi& epi) {
     if constexpr (P16 < NR16) {
       constexpr bool first = PRO && (P16 == 0);
-      constexpr bool last = EPI && (P16 == NR16 - 1) && (REM == 0);
-      pass<16, SIGN, first, last>(cx, buf, Ns, pro, epi);
-      passes16<SIGN, PRO, EPI, P16 + 1>(cx, buf, Ns * 16, pro, epi);
+      constexpr bool last_pass = (P16 == NR16 - 1) && (REM == 0);
+      constexpr bool last = EPI && last_pass;
+      pass<RADIX, SIGN, first, last>(cx, P16 == 0 ? src : buf, last_pass ? dst : buf, Ns, pro, epi);
+      passes<SIGN, PRO, EPI, P16 + 1>(cx, src, buf, dst, Ns * RADIX, pro, epi);
     } else if constexpr (REM > 0) {
-      pass<(1 << REM), SIGN, false, EPI>(cx, buf, Ns, pro, epi);
+      pass<(1 << REM), SIGN, false, EPI>(cx, buf, dst, Ns, pro, epi);
     }
   }
 
+  // M-point Stockham transform of the CTA's own slice: src -> (buf) -> dst.
   template <int SIGN, bool PRO, bool EPI, class Pro, class Epi>
-  static __device__ __forceinline__ void local_fft(const Ctx& cx, V* buf, Pro& pro, Epi& epi) {
-    passes16<SIGN, PRO, EPI, 0>(cx, buf, 1, pro, epi);
+  static __device__ __forceinline__ void local_fft(const Ctx& cx, const V* src, V* buf, V* dst, Pro& pro,
+                                                   Epi& epi) {
+    passes<SIGN, PRO, EPI, 0>(cx, src, buf, dst, 1, pro, epi);
   }
 
-  // Forward cross-CTA pass: slot n2 of every CTA r (= x[r*M + n2]) -> radix-C
-  // DFT -> twiddle W_N^{n2 k1} -> slot n2 of CTA k1.
+  // Forward cross-CTA pass, streaming into the exchange buffers: slot n2 of
+  // every CTA r (= x[r*M + n2], from pro) -> radix-C DFT -> twiddle W_N^{n2 k1}
+  // -> exchange slot n2 of CTA k1.  lead: a cluster barrier is needed first
+  // (inputs written since the last one).
   template <class Pro>
-  static __device__ __forceinline__ void cross_fwd(const Ctx& cx, V* buf, Pro& pro) {
+  static __device__ __forceinline__ void cross_fwd(const Ctx& cx, Pro& pro, bool lead) {
     constexpr int PM = M / C;
-    constexpr int BP = (PM + T - 1) / T;
-    V v[BP][C];
-    csync();
+    if constexpr (INPLACE) {
+      // in place: all reads, cluster barrier, all writes (into cx.W == cx.X)
+      constexpr int BP = (PM + T - 1) / T;
+      V v[BP][C];
+      csync();
 #pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
-      if (PM % T == 0 || q < PM) {
-        const int n2 = cx.rank * PM + q;
+      for (int b = 0; b < BP; ++b) {
+        const int q = threadIdx.x + b * T;
+        if (PM % T == 0 || q < PM)
 #pragma unroll
-        for (int r = 0; r < C; ++r) v[b][r] = pro(r, n2);
+          for (int r = 0; r < C; ++r) v[b][r] = pro(r, cx.rank * PM + q);
       }
-    }
-    csync();
+      csync();
 #pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
-      if (PM % T == 0 || q < PM) {
-        const int n2 = cx.rank * PM + q;
-        dft<C, +1>(v[b]);
+      for (int b = 0; b < BP; ++b) {
+        const int q = threadIdx.x + b * T;
+        if (PM % T == 0 || q < PM) {
+          const int n2 = cx.rank * PM + q;
+          dft<C, +1>(v[b]);
 #pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) {
-          V val = k1 ? cmul(v[b][k1], twid(cx.tw, n2 * k1, +1)) : v[b][k1];
-          rmt(buf, k1)[pad(n2)] = val;
+          for (int k1 = 0; k1 < C; ++k1)
+            rmt(cx.W, k1)[pad(n2)] = k1 ? cmul(v[b][k1], twid(cx.tw, n2 * k1, +1)) : v[b][k1];
         }
       }
+      csync();
+      return;
+    }
+    if (lead) csync();
+    for (int q = threadIdx.x; q < PM; q += T) {
+      const int n2 = cx.rank * PM + q;
+      V v[C];
+#pragma unroll
+      for (int r = 0; r < C; ++r) v[r] = pro(r, n2);
+      dft<C, +1>(v);
+#pragma unroll
+      for (int k1 = 0; k1 < C; ++k1) {
+        const V val = k1 ? cmul(v[k1], twid(cx.tw, n2 * k1, +1)) : v[k1];
+        rmt(cx.W, k1)[pad(n2)] = val;
+      }
     }
     csync();
   }
 
-  // Inverse cross-CTA pass: slot n2 of every CTA k1 -> twiddle W_N^{-n2 k1}
-  // -> radix-C DFT -> epi(n1, n2, x[n1*M + n2]).
+  // Inverse cross-CTA pass from the exchange buffers: exchange slot n2 of
+  // every CTA k1 -> twiddle W_N^{-n2 k1} -> radix-C DFT -> epi(n1, n2, x[n1*M + n2]).
   template <class Epi>
-  static __device__ __forceinline__ void cross_inv(const Ctx& cx, V* buf, Epi& epi) {
+  static __device__ __forceinline__ void cross_inv(const Ctx& cx, Epi& epi) {
     constexpr int PM = M / C;
-    constexpr int BP = (PM + T - 1) / T;
-    V v[BP][C];
-    csync();
+    if constexpr (INPLACE) {
+      constexpr int BP = (PM + T - 1) / T;
+      V v[BP][C];
+      csync();
 #pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
-      if (PM % T == 0 || q < PM) {
-        const int n2 = cx.rank * PM + q;
+      for (int b = 0; b < BP; ++b) {
+        const int q = threadIdx.x + b * T;
+        if (PM % T == 0 || q < PM)
 #pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) v[b][k1] = rmt(buf, k1)[pad(n2)];
+          for (int k1 = 0; k1 < C; ++k1) v[b][k1] = rmt(cx.W, k1)[pad(cx.rank * PM + q)];
       }
+      csync();
+#pragma unroll
+      for (int b = 0; b < BP; ++b) {
+        const int q = threadIdx.x + b * T;
+        if (PM % T == 0 || q < PM) {
+          const int n2 = cx.rank * PM + q;
+#pragma unroll
+          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+          dft<C, -1>(v[b]);
+#pragma unroll
+          for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
+        }
+      }
+      csync();
+      return;
     }
     csync();
+    for (int q = threadIdx.x; q < PM; q += T) {
+      const int n2 = cx.rank * PM + q;
+      V v[C];
 #pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
-      if (PM % T == 0 || q < PM) {
-        const int n2 = cx.rank * PM + q;
+      for (int k1 = 0; k1 < C; ++k1) v[k1] = rmt(cx.W, k1)[pad(n2)];
 #pragma unroll
-        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
-        dft<C, -1>(v[b]);
+      for (int k1 = 1; k1 < C; ++k1) v[k1] = cmul(v[k1], twid(cx.tw, n2 * k1, -1));
+      dft<C, -1>(v);
 #pragma unroll
-        for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
-      }
+      for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[n1]);
     }
     csync();
   }
 
-  // Forward transform G+(x)[k] = sum_n x[n] e^{+2 pi i k n / N} (= N * pyofss fft).
-  // pro(owner, slot): time-domain input; epi(owner, slot, v): spectral output,
-  // always called in the owner CTA.
+  // Forward transform G+(x)[k] = sum_n x[n] e^{+2 pi i k n / N} (= N * pyofss fft),
+  // result in buf (or to epi).  pro(owner, slot): time-domain input; epi(owner,
+  // slot, v): spectral output, always called in the owner CTA.  lead: inputs
+  // were written (locally) since the last cluster barrier.
   template <class Pro, class Epi>
-  static __device__ __forceinline__ void fwd(const Ctx& cx, V* buf, Pro& pro, Epi& epi) {
+  static __device__ __forceinline__ void fwd(const Ctx& cx, V* buf, Pro& pro, Epi& epi, bool lead = true) {
     if constexpr (C == 1) {
-      local_fft<+1, true, true>(cx, buf, pro, epi);
+      local_fft<+1, true, true>(cx, buf, buf, buf, pro, epi);
     } else {
-      cross_fwd(cx, buf, pro);
-      local_fft<+1, false, true>(cx, buf, pro, epi);
+      cross_fwd(cx, pro, lead);
+      local_fft<+1, false, true>(cx, cx.W, buf, buf, pro, epi);
     }
   }
 
@@ -332,10 +382,10 @@ struct Engine {
   template <class Pro, class Epi>
   static __device__ __forceinline__ void inv(const Ctx& cx, V* buf, Pro& pro, Epi& epi) {
     if constexpr (C == 1) {
-      local_fft<-1, true, true>(cx, buf, pro, epi);
+      local_fft<-1, true, true>(cx, buf, buf, buf, pro, epi);
     } else {
-      local_fft<-1, true, false>(cx, buf, pro, epi);
-      cross_inv(cx, buf, epi);
+      local_fft<-1, true, false>(cx, buf, buf, cx.W, pro, epi);
+      cross_inv(cx, epi);
     }
   }
 
@@ -449,7 +499,7 @@ struct Engine {
       const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
       auto rdP = [&](int o, int l) -> V { return rmt(P, o)[pad(l)]; };
       auto wrP = [&](int o, int l, V v) { P[pad(l)] = v; };
-      fwd(cx, P, rdP, wrP);
+      fwd(cx, P, rdP, wrP, false);  // inv() ended with a cluster barrier
 #if GNLSE_RAMAN_SPLIT
       // spectral product and time-domain combination as separate passes over
       // this CTA's slice (fewer live registers in the transform passes)
@@ -475,7 +525,7 @@ struct Engine {
 #endif
     }
     auto wrX = [&](int o, int l, V v) { X[pad(l)] = v; };
-    fwd(cx, X, rdX, wrX);
+    fwd(cx, X, rdX, wrX, GNLSE_RAMAN_SPLIT && raman);  // inputs last written by inv() otherwise
     return energy;
   }
 
@@ -506,11 +556,12 @@ struct Engine {
   // The extended-state mode runs them in FP64, reusing the complex128
   // transform code on the same shared memory (X and P together hold one
   // double2 slice of M padded points).
-  using E64 = Engine<double, LOGM, C, false>;
+  using E64 = Engine<double, LOGM, C, false, true>;
   static __device__ __forceinline__ typename E64::Ctx ctx64(const Ctx& cx, const GridDev& g) {
     typename E64::Ctx c;
     c.X = reinterpret_cast<double2*>(cx.X);
     c.P = c.X;
+    c.W = c.X;  // in-place cross passes
     c.red = cx.red;
     c.tw = (const double2*)g.tw64;
     c.twl = (const double2*)g.twl64;
@@ -828,7 +879,8 @@ struct Engine {
     Ctx cx;
     cx.X = (V*)smem_raw;
     cx.P = cx.X + MP;
-    cx.red = (double*)(cx.P + MP);
+    cx.W = C > 1 ? cx.P + MP : nullptr;
+    cx.red = (double*)(cx.X + NBUF * MP);
     Ctl& c = *(Ctl*)(cx.red + RED);
     if constexpr (C > 1) {
       cx.rank = (int)cg::this_cluster().block_rank();

@@ -1,0 +1,3 @@
+// Kernel instantiation: extended-state complex64, M = 2^11 points per CTA, cluster of 4.
+#include "gnlse_inst.inc"
+GNLSE_INSTANTIATE_MIX(11, 4)

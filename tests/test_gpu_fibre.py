@@ -32,7 +32,9 @@ def test_system_with_cuda_fibre(cuda_ready, name, precision, tol):
     out = sys_.fields["fibre"]
     assert spec_err(out, case["A_out"]) <= tol
     st = sys_["fibre"].stepper
-    np.testing.assert_allclose(st.storage.z, case["trace_z"], rtol=1e-9)
+    # mixed plans estimate the local error from complex64 stages, so accepted
+    # step sizes (and trace positions) follow FP64 only to ~1e-4 relative
+    np.testing.assert_allclose(st.storage.z, case["trace_z"], rtol=1e-9 if precision == "fp64" else 2e-3)
 
 
 def test_fibre_raises_reference_exception(cuda_ready):
