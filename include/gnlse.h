@@ -171,6 +171,23 @@ int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t*
 /* Copy per-instance statistics to host memory (synchronises `stream`). */
 int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
 
+/* Propagate one complex64 field of 256..4096 points (power of two) without
+ * allocating any memory.  No counterpart in the reference: pyofss has no GPU
+ * path of this kind.  It serves callers that must not allocate device memory
+ * while they propagate -- a host loop sharing the GPU with latency-critical
+ * work (cudaMalloc/cudaFree synchronise the device), or a process whose device
+ * memory is owned by another allocator or quota.  Tables, scratch and control
+ * state live in one file-scope device array of 545 KiB that every GPU loading
+ * the library keeps until exit; the caller passes the grid's host tables, the
+ * instance description (max_traces must be 0) and the field d_field (device,
+ * in place).  Larger grids return GNLSE_UNSUPPORTED.  All calls share the
+ * array: calls whose GPU work overlaps (other streams or threads) race and
+ * must be serialised by the caller.  The first call on each device looks up
+ * the array's address; make it before any stream capture.  The call waits for
+ * its host-to-device table copies; stats_out (optional) waits for the result. */
+int gnlse_propagate_noalloc(const gnlse_grid_desc* grid, const gnlse_instance_desc* instance,
+                            void* d_field, gnlse_stats* stats_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

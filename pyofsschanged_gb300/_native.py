@@ -85,6 +85,8 @@ SIGNATURES = {
     "gnlse_propagate_host": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "gnlse_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
     "gnlse_set_timing": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "gnlse_propagate_noalloc": (ct.c_int, [ct.POINTER(GridDesc), ct.POINTER(InstanceDesc),
+                                           ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
     "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
