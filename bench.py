@@ -45,6 +45,11 @@ def parse():
                     help="members re-solved in FP64 on the GPU to state the spectral error")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-attempts", type=int, default=20,
+                    help="attempts per grid size timed on the plain single-instance GPU path")
+    ap.add_argument("--cluster", default="",
+                    help="cluster size per grid size, e.g. '16384:4,8192:2' (default: the "
+                         "library's choice)")
     ap.add_argument("--profile-attempts", type=int, default=0,
                     help="profiling only: run W+K launches of at most this many attempts per "
                          "member and exit (short kernels for ncu); prints no bench line")
@@ -215,7 +220,8 @@ def run_ours(a):
     from pyofsschanged_gb300.ensemble import ensemble_plan_inputs, sc_ensemble
 
     members, domains, fields = sc_ensemble(a.members)
-    grids, inst = ensemble_plan_inputs(members, domains)
+    cluster = {int(k): int(v) for k, v in (kv.split(":") for kv in a.cluster.split(",") if kv)}
+    grids, inst = ensemble_plan_inputs(members, domains, cluster=cluster)
     plan = Plan(grids, inst, precision=a.precision, device=local)
     src = plan.pack(fields)
     work = torch.empty_like(src)
@@ -341,6 +347,32 @@ def run_ours(a):
         acc = {"members": len(idx), "median": statistics.median(errs), "max": max(errs),
                "frac_le_1e-4": sum(e <= 1e-4 for e in errs) / len(errs)}
 
+    # plain single-instance GPU path (one library call per reference operation),
+    # bounded per-attempt samples per grid size x this run's per-member attempt counts
+    plain = None
+    if rank == 0 and a.plain_attempts > 0:
+        from pyofsschanged_gb300.ensemble import FIBRE_835
+        from pyofsschanged_gb300.operators import GridTables
+        from pyofsschanged_gb300.plain import PlainRK4IP
+        per_att = {}
+        for n in sorted(domains):
+            i = next(k for k, m in enumerate(members) if m.n == n)
+            pp = PlainRK4IP(GridTables(domains[n], **FIBRE_835), members[i].length)
+            a0 = torch.as_tensor(fields[i]).to(dev)
+            pp.adaptive(a0, 1e-6, max_attempts=2)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, att, _ = pp.adaptive(a0, 1e-6, max_attempts=a.plain_attempts)
+            torch.cuda.synchronize()
+            per_att[n] = (time.perf_counter() - t0) / att
+        t_solve = [s["attempts"] * per_att[plan.grids[plan.instances[i].grid].n]
+                   for i, s in enumerate(stats)]
+        pv = 1.0 / (sum(t_solve) / len(t_solve))
+        plain = {"value": pv, "unit": UNIT, "fused_over_plain": value / pv,
+                 "sample": f"{a.plain_attempts} ARK4IP attempts per grid size, complex128, "
+                           "torch.fft/cuFFT per reference fft call, host read-back per attempt",
+                 "s_per_attempt": {str(k): v for k, v in per_att.items()}}
+
     if rank == 0 and not a.no_cpu:
         per_att, wall, tot, jobs = cpu_sample(a.members, os.cpu_count() or 1, a.cpu_sample_s)
         attempts = [s["attempts"] for s in stats]
@@ -362,7 +394,7 @@ def run_ours(a):
                        "l2": "256 MiB buffer written between steps",
                        "evals_per_step": evals},
             "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
-            "gpu_launches": launches, "accuracy_vs_fp64": acc,
+            "gpu_launches": launches, "accuracy_vs_fp64": acc, "plain": plain,
             "class_ms": {f"m2^{k[0]}_c{k[1]}_n{k[2]}": statistics.mean(v) for k, v in per_cls.items()}}
     if rank == 0:
         print(json.dumps(line))

@@ -101,6 +101,8 @@ typedef struct {
   double length;              /* km */
   double local_error;         /* adaptive tolerance */
   double h0;                  /* adaptive initial step, km; <= 0: the stepper's rule */
+  double weight;              /* expected relative work (e.g. predicted attempts) used to
+                                 start long propagations first; <= 0: the fibre length */
 } gnlse_instance_desc;
 
 typedef struct {
@@ -168,6 +170,11 @@ int gnlse_set_timing(gnlse_plan* plan, int enable);
 int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t* cluster,
                       int32_t* count, double* ms);
 
+/* Phase cycle counters of builds compiled with GNLSE_PROF=1 (8 per instance:
+ * transforms, stage loops, exp(hD) tables, whole kernel); GNLSE_UNSUPPORTED
+ * in normal builds.  Synchronises the device. */
+int gnlse_profile_counters(gnlse_plan* plan, long long* out);
+
 /* Copy per-instance statistics to host memory (synchronises `stream`). */
 int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
 
@@ -177,7 +184,7 @@ int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
  * while they propagate -- a host loop sharing the GPU with latency-critical
  * work (cudaMalloc/cudaFree synchronise the device), or a process whose device
  * memory is owned by another allocator or quota.  Tables, scratch and control
- * state live in one file-scope device array of 545 KiB that every GPU loading
+ * state live in one file-scope device array of 585 KiB that every GPU loading
  * the library keeps until exit; the caller passes the grid's host tables, the
  * instance description (max_traces must be 0) and the field d_field (device,
  * in place).  Larger grids return GNLSE_UNSUPPORTED.  All calls share the

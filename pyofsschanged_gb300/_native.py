@@ -47,6 +47,7 @@ class InstanceDesc(ct.Structure):
         ("grid", ct.c_int32), ("method", ct.c_int32), ("total_steps", ct.c_int32),
         ("traces", ct.c_int32), ("max_traces", ct.c_int32), ("pad0", ct.c_int32),
         ("length", ct.c_double), ("local_error", ct.c_double), ("h0", ct.c_double),
+        ("weight", ct.c_double),
     ]
 
 
@@ -85,12 +86,15 @@ SIGNATURES = {
     "gnlse_propagate_host": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "gnlse_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
     "gnlse_set_timing": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "gnlse_profile_counters": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_longlong)]),
     "gnlse_propagate_noalloc": (ct.c_int, [ct.POINTER(GridDesc), ct.POINTER(InstanceDesc),
                                            ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
     "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
 }
+
+OPTIONAL = {"gnlse_propagate_noalloc"}
 
 _lib = None
 _lock = threading.Lock()
@@ -115,6 +119,8 @@ def load(path=LIB_PATH):
                 "`python -m pyofsschanged_gb300.build` (no CPU fallback exists)")
         lib = ct.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
+            if name in OPTIONAL and not hasattr(lib, name):
+                continue  # reduced tuning builds leave these out
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args

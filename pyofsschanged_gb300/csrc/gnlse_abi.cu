@@ -11,17 +11,36 @@
 
 #include "../../include/gnlse.h"
 #include "gnlse_launch.h"
+#include "gnlse_twiddle.h"
 #include "gnlse_types.h"
 
 using namespace gnlse;
 
 namespace {
 
+// One kernel launch: the instances order[first, first + count) of one
+// (points per CTA, cluster size) class at one start-priority level.
 struct ClassRun {
   int logm, C;
   int first;  // offset into the order array
   int count;
+  int level;  // 0 = longest predicted propagations (highest stream priority)
 };
+
+// Predicted per-attempt latency (relative units) of a field in class (logm, C):
+// measured GB300 transform times per cluster, 44 transforms per attempt.
+double attempt_cost(int logm, int C, int precision) {
+  const int M = 1 << logm;
+  double t;
+  if (logm == 12 && C == 1) t = 2.2;
+  else if (logm == 12 && C == 2) t = 4.0;
+  else if (logm == 12 && C == 4) t = 9.2;
+  else if (logm == 11 && C == 2) t = 2.3;
+  else if (logm == 11 && C == 4) t = 4.0;
+  else if (logm == 11 && C == 8) t = 4.5;
+  else t = 2.2 * (M / 4096.0) * (logm / 12.0) * (C > 1 ? 1.0 + 0.5 * std::log2((double)C) : 1.0);
+  return precision == GNLSE_FP64 ? 30.0 * t : t;
+}
 
 struct GridHost {
   int n, logm, C;
@@ -35,6 +54,8 @@ struct GridHost {
   void* d_tw64 = nullptr;
   void* d_twl64 = nullptr;
   void* d_cis = nullptr;
+  void* d_twp = nullptr;
+  void* d_twp64 = nullptr;
 };
 
 bool supported(int precision, int logm, int C) {
@@ -98,6 +119,7 @@ struct gnlse_plan {
   std::vector<cudaEvent_t> ev;
   cudaEvent_t fork = nullptr;
   bool timing = false;
+  long long* d_prof = nullptr;  // phase cycle counters (profiling builds)
   std::vector<cudaEvent_t> t0, t1;
   // host-buffer entry point staging
   void* d_io = nullptr;
@@ -158,7 +180,24 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
     twl[2 * (size_t)j] = tw[2 * (size_t)j * C];
     twl[2 * (size_t)j + 1] = tw[2 * (size_t)j * C + 1];
   }
+  // per-pass twiddle rows of the M-point transform
+  const int logm = gh.logm, ntwp = twp_size(logm, GNLSE_RADIX_BITS);
+  std::vector<R> twp(2 * (size_t)ntwp);
+  std::vector<double> twp64(extended ? 2 * (size_t)ntwp : 0);
+  for (int e2 = 0; e2 < ntwp; ++e2) {
+    const long double ang = 2.0L * 3.14159265358979323846264338327950288L *
+                            (long double)twp_exponent(logm, GNLSE_RADIX_BITS, e2) / (long double)M;
+    const double c = (double)cosl(ang), sn = (double)sinl(ang);
+    twp[2 * (size_t)e2] = (R)c;
+    twp[2 * (size_t)e2 + 1] = (R)sn;
+    if (extended) {
+      twp64[2 * (size_t)e2] = c;
+      twp64[2 * (size_t)e2 + 1] = sn;
+    }
+  }
   cudaError_t e;
+  if ((e = upload(p, twp, &gh.d_twp)) != cudaSuccess) return e;
+  if (extended && (e = upload(p, twp64, &gh.d_twp64)) != cudaSuccess) return e;
   if (extended) {
     // FP64 twiddles for the boundary transforms and the double-float
     // cis(j pi/512) table of the exp(hD) factors
@@ -204,6 +243,8 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   dv.tw64 = gh.d_tw64;
   dv.twl64 = gh.d_twl64;
   dv.cis_df = gh.d_cis;
+  dv.twp = gh.d_twp;
+  dv.twp64 = gh.d_twp64;
   dv.n = n;
   dv.logm = gh.logm;
   dv.C = C;
@@ -277,7 +318,12 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     // 4096 (complex128: one CTA per SM); larger grids span a cluster
     const int mmax = 4096;
     if (C == 0) {
+      // Measured per-transform cost (GB300, complex64): the cross-CTA exchange
+      // through distributed shared memory costs more per byte than the local
+      // passes, so a 2^14 field runs fastest as 8 CTAs x 2048 points (4.5 us
+      // per transform) rather than 4 x 4096 (9.2 us); 2^13 as 2 x 4096.
       C = n <= mmax ? 1 : n / mmax;
+      if (precision != GNLSE_FP64 && n == 4 * mmax) C = 8;
       if (C > 8) C = n / (2 * mmax);  // complex64 2^16: 8 CTAs of 8192 points
     }
     if (C != 1 && C != 2 && C != 4 && C != 8) {
@@ -346,24 +392,35 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   p->trace_elems = toff;
   p->tracez_elems = zoff;
   p->scratch_bytes = (size_t)soff * p->ssize;
-  // classes: instances grouped by (logm, C), longest estimated work first
+  // Launch schedule: predicted duration = work weight x per-attempt cost of the
+  // instance's class.  Instances whose predicted duration is within 60% of the
+  // longest start at level 0, down to 30% at level 1, the rest at level 2; each
+  // (level, class) pair is one launch, and levels map to decreasing stream
+  // priorities, so long propagations of every grid size get SMs first
+  // (longest-processing-time-first across the launches).
   std::vector<int> ids(n_instances);
-  for (int i = 0; i < n_instances; ++i) ids[i] = i;
-  auto cls = [&](int i) { const GridHost& g = p->grids[p->inst[i].grid]; return g.logm * 16 + g.C; };
-  auto cost = [&](int i) {
+  std::vector<double> dur(n_instances);
+  double dmax = 0.0;
+  for (int i = 0; i < n_instances; ++i) {
+    ids[i] = i;
     const GridHost& g = p->grids[p->inst[i].grid];
-    return p->inst[i].length * (double)g.n * std::log2((double)g.n);
-  };
+    const double w = instances[i].weight > 0 ? instances[i].weight : p->inst[i].length;
+    dur[i] = w * attempt_cost(g.logm, g.C, precision);
+    dmax = std::max(dmax, dur[i]);
+  }
+  auto level = [&](int i) { return dur[i] >= 0.6 * dmax ? 0 : (dur[i] >= 0.3 * dmax ? 1 : 2); };
+  auto cls = [&](int i) { const GridHost& g = p->grids[p->inst[i].grid]; return g.logm * 16 + g.C; };
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) {
+    if (level(a) != level(b)) return level(a) < level(b);
     if (cls(a) != cls(b)) return cls(a) < cls(b);
-    return cost(a) > cost(b);
+    return dur[a] > dur[b];
   });
   p->order = ids;
   for (int k = 0; k < n_instances;) {
     int j = k;
-    while (j < n_instances && cls(ids[j]) == cls(ids[k])) ++j;
+    while (j < n_instances && cls(ids[j]) == cls(ids[k]) && level(ids[j]) == level(ids[k])) ++j;
     const GridHost& g = p->grids[p->inst[ids[k]].grid];
-    p->classes.push_back({g.logm, g.C, k, j - k});
+    p->classes.push_back({g.logm, g.C, k, j - k, level(ids[k])});
     k = j;
   }
   cudaError_t e;
@@ -380,10 +437,23 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   cudaMemset(p->d_state, 0, sizeof(InstState) * n_instances);
   if ((e = cudaMalloc(&p->d_scratch, p->scratch_bytes)) != cudaSuccess) { free_plan(p); return cuda_fail(e); }
   p->allocs.push_back(p->d_scratch);
+#if GNLSE_PROF
+  if ((e = cudaMalloc((void**)&p->d_prof, sizeof(long long) * 8 * n_instances)) != cudaSuccess) {
+    free_plan(p);
+    return cuda_fail(e);
+  }
+  p->allocs.push_back(p->d_prof);
+  cudaMemset(p->d_prof, 0, sizeof(long long) * 8 * n_instances);
+#endif
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
   for (size_t c = 0; c < p->classes.size(); ++c) {
     cudaStream_t s;
     cudaEvent_t ev;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+    // level 0 -> greatest priority (numerically lowest), then one step per level
+    int prio = prio_greatest + p->classes[c].level;
+    if (prio > prio_least) prio = prio_least;
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio) != cudaSuccess ||
         cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
       free_plan(p);
       return GNLSE_CUDA_ERROR;
@@ -448,6 +518,7 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
   kp.traces = d_traces;
   kp.trace_z = d_trace_z;
   kp.max_attempts = max_attempts;
+  kp.prof = p->d_prof;
   cudaError_t e;
   if (p->classes.size() == 1) {
     const ClassRun& c = p->classes[0];
@@ -497,6 +568,15 @@ int gnlse_propagate_host(gnlse_plan* p, const void* h_in, void* h_out, void* str
   if (rc != GNLSE_OK) return rc;
   if ((e = cudaMemcpyAsync(h_out, p->d_io, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_fail(e);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
+  return GNLSE_OK;
+}
+
+int gnlse_profile_counters(gnlse_plan* p, long long* out) {
+  if (!p || !out) return GNLSE_BAD_ARGUMENT;
+  if (!p->d_prof) return GNLSE_UNSUPPORTED;
+  cudaDeviceSynchronize();
+  if (cudaMemcpy(out, p->d_prof, sizeof(long long) * 8 * p->inst.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GNLSE_CUDA_ERROR;
   return GNLSE_OK;
 }
 

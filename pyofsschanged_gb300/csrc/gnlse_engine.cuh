@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "gnlse_df.cuh"
+#include "gnlse_twiddle.h"
 #include "gnlse_types.h"
 
 #ifndef GNLSE_MINB_CAP
@@ -33,16 +34,26 @@
 #ifndef GNLSE_RAMAN_SPLIT
 #define GNLSE_RAMAN_SPLIT 0
 #endif
-// log2 of the radix of the Stockham passes (3: radix 8, 4: radix 16) and the
-// points each thread holds per pass
-#ifndef GNLSE_RADIX_BITS
-#define GNLSE_RADIX_BITS 4
-#endif
+// points each thread holds per pass (the radix is set in gnlse_twiddle.h)
 #ifndef GNLSE_PPT
 #define GNLSE_PPT 16
 #endif
 
 namespace cg = cooperative_groups;
+
+// Phase cycle counters (GNLSE_PROF builds): thread 0 of each cluster's first
+// CTA accumulates clock64() deltas of the attempt's phases into kp.prof.
+#ifndef GNLSE_PROF
+#define GNLSE_PROF 0
+#endif
+#if GNLSE_PROF
+#define PROF_T0() long long _pt0 = clock64()
+#define PROF_ADD(k) \
+  do { if (threadIdx.x == 0) prof_acc[k] += clock64() - _pt0; _pt0 = clock64(); } while (0)
+#else
+#define PROF_T0() do {} while (0)
+#define PROF_ADD(k) do {} while (0)
+#endif
 
 namespace gnlse {
 
@@ -146,7 +157,7 @@ struct Engine {
   static constexpr int N = M * C;
   static constexpr int T = (M / GNLSE_PPT) < 64 ? 64 : (M / GNLSE_PPT);
   static constexpr int MP = M + M / 16;
-  static constexpr int RB = GNLSE_RADIX_BITS;  // log2 of the main radix
+  static constexpr int RB = GNLSE_RADIX_BITS;  // log2 of the main radix (gnlse_twiddle.h)
   static constexpr int RADIX = 1 << RB;
   static constexpr int NR16 = LOGM / RB;        // passes of the main radix
   static constexpr int REM = LOGM % RB;         // log2 of the final smaller radix
@@ -171,7 +182,8 @@ struct Engine {
     V* W;          // exchange buffer of the cross-CTA passes (C > 1)
     double* red;
     const V* tw;   // N-point table (cross-CTA pass)
-    const V* twl;  // M-point table (per-CTA passes)
+    const V* twl;  // M-point table
+    const V* twp;  // per-pass twiddle rows (per-CTA passes)
     int rank;
   };
 
@@ -201,7 +213,23 @@ struct Engine {
   // One radix-RAD Stockham pass over the CTA's M points: all loads, barrier,
   // all stores (so src may equal dst).  FIRST: inputs from pro(owner, slot),
   // otherwise from src; LAST: outputs to epi(owner, slot, v), otherwise to dst.
-  template <int RAD, int SIGN, bool FIRST, bool LAST, class Pro, class Epi>
+  // twiddles of one butterfly: row[r] = W^{r k ...}, r < RAD, one 128-bit load per 16 bytes
+  template <int RAD>
+  static __device__ __forceinline__ void load_row(const V* row, V (&w)[RAD]) {
+    if constexpr (sizeof(V) == 8) {
+#pragma unroll
+      for (int i = 0; i < RAD / 2; ++i) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(row) + i);
+        w[2 * i] = mk<V>(q.x, q.y);
+        w[2 * i + 1] = mk<V>(q.z, q.w);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) w[r] = __ldg(row + r);
+    }
+  }
+
+  template <int RAD, int SIGN, bool FIRST, bool LAST, int OFF, class Pro, class Epi>
   static __device__ __forceinline__ void pass(const Ctx& cx, const V* src, V* dst, int Ns, Pro& pro,
                                               Epi& epi) {
     constexpr int NB = M / RAD;
@@ -227,9 +255,10 @@ struct Engine {
       if (NB % T == 0 || j < NB) {
         const int k = j & (Ns - 1);
         if (Ns > 1) {
-          const int step = k * (M / (Ns * RAD));
+          V w[RAD];
+          load_row<RAD>(cx.twp + OFF + k * RAD, w);
 #pragma unroll
-          for (int r = 1; r < RAD; ++r) v[b][r] = cmul(v[b][r], twid(cx.twl, r * step, SIGN));
+          for (int r = 1; r < RAD; ++r) v[b][r] = SIGN > 0 ? cmul(v[b][r], w[r]) : cmulc(v[b][r], w[r]);
         }
         dft<RAD, SIGN>(v[b]);
         const int base = (j - k) * RAD + k;
@@ -251,10 +280,11 @@ struct Engine {
       constexpr bool first = PRO && (P16 == 0);
       constexpr bool last_pass = (P16 == NR16 - 1) && (REM == 0);
       constexpr bool last = EPI && last_pass;
-      pass<RADIX, SIGN, first, last>(cx, P16 == 0 ? src : buf, last_pass ? dst : buf, Ns, pro, epi);
+      pass<RADIX, SIGN, first, last, twp_offset(LOGM, RB, P16)>(cx, P16 == 0 ? src : buf,
+                                                                 last_pass ? dst : buf, Ns, pro, epi);
       passes<SIGN, PRO, EPI, P16 + 1>(cx, src, buf, dst, Ns * RADIX, pro, epi);
     } else if constexpr (REM > 0) {
-      pass<(1 << REM), SIGN, false, EPI>(cx, buf, dst, Ns, pro, epi);
+      pass<(1 << REM), SIGN, false, EPI, twp_offset(LOGM, RB, NR16)>(cx, buf, dst, Ns, pro, epi);
     }
   }
 
@@ -300,16 +330,27 @@ struct Engine {
       return;
     }
     if (lead) csync();
-    for (int q = threadIdx.x; q < PM; q += T) {
-      const int n2 = cx.rank * PM + q;
-      V v[C];
+    // all positions of a thread at once, so their remote loads overlap
+    constexpr int BP = (PM + T - 1) / T;
+    V v[BP][C];
 #pragma unroll
-      for (int r = 0; r < C; ++r) v[r] = pro(r, n2);
-      dft<C, +1>(v);
+    for (int b = 0; b < BP; ++b) {
+      const int q = threadIdx.x + b * T;
+      if (PM % T == 0 || q < PM)
 #pragma unroll
-      for (int k1 = 0; k1 < C; ++k1) {
-        const V val = k1 ? cmul(v[k1], twid(cx.tw, n2 * k1, +1)) : v[k1];
-        rmt(cx.W, k1)[pad(n2)] = val;
+        for (int r = 0; r < C; ++r) v[b][r] = pro(r, cx.rank * PM + q);
+    }
+#pragma unroll
+    for (int b = 0; b < BP; ++b) {
+      const int q = threadIdx.x + b * T;
+      if (PM % T == 0 || q < PM) {
+        const int n2 = cx.rank * PM + q;
+        dft<C, +1>(v[b]);
+#pragma unroll
+        for (int k1 = 0; k1 < C; ++k1) {
+          const V val = k1 ? cmul(v[b][k1], twid(cx.tw, n2 * k1, +1)) : v[b][k1];
+          rmt(cx.W, k1)[pad(n2)] = val;
+        }
       }
     }
     csync();
@@ -348,16 +389,26 @@ struct Engine {
       return;
     }
     csync();
-    for (int q = threadIdx.x; q < PM; q += T) {
-      const int n2 = cx.rank * PM + q;
-      V v[C];
+    constexpr int BP = (PM + T - 1) / T;
+    V v[BP][C];
 #pragma unroll
-      for (int k1 = 0; k1 < C; ++k1) v[k1] = rmt(cx.W, k1)[pad(n2)];
+    for (int b = 0; b < BP; ++b) {
+      const int q = threadIdx.x + b * T;
+      if (PM % T == 0 || q < PM)
 #pragma unroll
-      for (int k1 = 1; k1 < C; ++k1) v[k1] = cmul(v[k1], twid(cx.tw, n2 * k1, -1));
-      dft<C, -1>(v);
+        for (int k1 = 0; k1 < C; ++k1) v[b][k1] = rmt(cx.W, k1)[pad(cx.rank * PM + q)];
+    }
 #pragma unroll
-      for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[n1]);
+    for (int b = 0; b < BP; ++b) {
+      const int q = threadIdx.x + b * T;
+      if (PM % T == 0 || q < PM) {
+        const int n2 = cx.rank * PM + q;
+#pragma unroll
+        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+        dft<C, -1>(v[b]);
+#pragma unroll
+        for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
+      }
     }
     csync();
   }
@@ -565,6 +616,7 @@ struct Engine {
     c.red = cx.red;
     c.tw = (const double2*)g.tw64;
     c.twl = (const double2*)g.twl64;
+    c.twp = (const double2*)g.twp64;
     c.rank = cx.rank;
     return c;
   }
@@ -903,9 +955,14 @@ struct Engine {
     Op& op = c.op;
     cx.tw = (const V*)g.tw;
     cx.twl = (const V*)g.twl;
+    cx.twp = (const V*)g.twp;
     FV* field = (FV*)kp.fields + d.field_off;
     SV* base = (SV*)kp.scratch + d.scratch_off;
     long long budget = kp.max_attempts > 0 ? kp.max_attempts : (1ll << 62);
+#if GNLSE_PROF
+    long long prof_acc[4] = {0, 0, 0, 0};
+    const long long prof_start = clock64();
+#endif
 
     if (st.phase == 0) {
       int ntr = 0, ovf = 0;
@@ -962,7 +1019,9 @@ struct Engine {
       if (st.phase != 1) break;
       const double h = adaptive ? st.h : d.length / d.total_steps;
       const int sidx = st.sidx;
+      PROF_T0();
       if (adaptive) exp_table(cx, g, 0.25 * h, base + 6 * N, base + 7 * N);
+      PROF_ADD(2);
       const int q_end = adaptive ? 11 : 4;
       double nrm[3] = {0.0, 0.0, 0.0};
       for (int q = st.ma_valid ? 1 : 0; q < q_end; ++q) {
@@ -996,7 +1055,9 @@ struct Engine {
         } else if (kind == 0) {
           load_state(cx, mi == 0 ? S : Sh);
         }
+        PROF_ADD(1);
         const double en = nonlinear(cx, g, kind == 0 && g.gain);
+        PROF_ADD(0);
         if (kind == 0) {
           V* MA = reinterpret_cast<V*>(base + (3 + mi) * N);
           store_ma(cx, g, MA);
@@ -1034,6 +1095,7 @@ struct Engine {
           post_stage3(cx, op, adaptive && q == 10, nrm);
           if (threadIdx.x == 0) st.evals += 1;
         }
+        PROF_ADD(1);
       }
       budget -= 1;
 
@@ -1124,6 +1186,12 @@ struct Engine {
     }
     __syncthreads();
     if (cx.rank == 0 && threadIdx.x == 0) kp.state[id] = st;
+#if GNLSE_PROF
+    if (kp.prof && cx.rank == 0 && threadIdx.x == 0) {
+      for (int k = 0; k < 3; ++k) kp.prof[8 * id + k] += prof_acc[k];
+      kp.prof[8 * id + 3] += clock64() - prof_start;
+    }
+#endif
   }
 };
 

@@ -25,13 +25,15 @@
 
 #include "../../include/gnlse.h"
 #include "gnlse_launch.h"
+#include "gnlse_twiddle.h"
 #include "gnlse_types.h"
 
 namespace {
 
 constexpr int kNoAllocMaxN = 4096;
 // layout (bytes, N = kNoAllocMaxN): scratch 8N complex64 | beta N f64 | nu N f64 |
-// Kr N f32 | lor N f32 | Hp N c64 | tw N c64 | staging ss/hR_re/hR_im/gain 4N f64 | control
+// Kr N f32 | lor N f32 | Hp N c64 | tw N c64 | staging ss/hR_re/hR_im/gain 4N f64 |
+// per-pass twiddle rows | control
 constexpr size_t kScratch = 8ull * kNoAllocMaxN * 8;
 constexpr size_t kBeta = kScratch;
 constexpr size_t kNu = kBeta + 8ull * kNoAllocMaxN;
@@ -40,8 +42,10 @@ constexpr size_t kLor = kKr + 4ull * kNoAllocMaxN;
 constexpr size_t kHp = kLor + 4ull * kNoAllocMaxN;
 constexpr size_t kTw = kHp + 8ull * kNoAllocMaxN;
 constexpr size_t kStage = kTw + 8ull * kNoAllocMaxN;
-constexpr size_t kCtl = kStage + 4ull * 8 * kNoAllocMaxN;
-constexpr size_t kNoAllocBytes = kCtl + 1024;  // 545 KiB in all
+constexpr size_t kTwp = kStage + 4ull * 8 * kNoAllocMaxN;
+constexpr int kTwpMax = 5120;  // >= twp_size(12, radix bits) for radix 8 and 16
+constexpr size_t kCtl = kTwp + 8ull * kTwpMax;
+constexpr size_t kNoAllocBytes = kCtl + 1024;  // 585 KiB in all
 
 static __device__ __align__(256) unsigned char g_noalloc[kNoAllocBytes];
 
@@ -60,6 +64,15 @@ __global__ void noalloc_tables(unsigned char* base, int n, double gamma, int has
   float* lor = (float*)(base + kLor);
   float2* Hp = (float2*)(base + kHp);
   float2* tw = (float2*)(base + kTw);
+  float2* twp = (float2*)(base + kTwp);
+  int logm = 0;
+  while ((1 << logm) < n) ++logm;
+  const int ntwp = gnlse::twp_size(logm, GNLSE_RADIX_BITS);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ntwp; e += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)gnlse::twp_exponent(logm, GNLSE_RADIX_BITS, e) / (double)n, &s, &c);
+    twp[e] = make_float2((float)c, (float)s);
+  }
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
     Kr[a] = (float)(gamma * (has_ss ? ss[a] : 1.0));
     if (raman) Hp[a] = make_float2((float)(hre[a] / n), (float)(him[a] / n));
@@ -119,6 +132,7 @@ extern "C" int gnlse_propagate_noalloc(const gnlse_grid_desc* gd, const gnlse_in
   if (raman && !gd->hR_im && e == cudaSuccess) e = cudaMemsetAsync(stage + 2 * kNoAllocMaxN, 0, nb, s);
   if (gain) put(stage + 3 * kNoAllocMaxN, gd->gain_profile, nb);  // none: flat profile
   if (e != cudaSuccess) return GNLSE_CUDA_ERROR;
+  static_assert(gnlse::twp_size(12, GNLSE_RADIX_BITS) <= kTwpMax, "twiddle rows");
   noalloc_tables<<<(n + 255) / 256, 256, 0, s>>>(base, n, gd->gamma, gd->ss_w != nullptr, raman, gain,
                                                   gd->gain_profile != nullptr);
   if (cudaGetLastError() != cudaSuccess) return GNLSE_CUDA_ERROR;
@@ -132,6 +146,7 @@ extern "C" int gnlse_propagate_noalloc(const gnlse_grid_desc* gd, const gnlse_in
   g.nu = (const double*)(base + kNu);
   g.tw = base + kTw;
   g.twl = base + kTw;
+  g.twp = base + kTwp;
   g.n = n;
   g.logm = 0;
   while ((1 << g.logm) < n) ++g.logm;

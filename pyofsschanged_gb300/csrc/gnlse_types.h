@@ -19,6 +19,8 @@ struct GridDev {
   const void* twl;      // [M] natural order: exp(+2 pi i j / M) (per-CTA transform)
   const void* tw64;     // extended-state plans: FP64 copies of tw and twl
   const void* twl64;
+  const void* twp;      // per-pass twiddle rows of the M-point transform (gnlse_twiddle.h)
+  const void* twp64;    // extended-state plans: FP64 copy of twp
   const void* cis_df;   // extended-state plans: [1024] double-float cis(j pi / 512)
   int n, logm, C, raman;
   int gain, pad0;
@@ -73,6 +75,7 @@ struct KParams {
   void* traces;         // base of trace slots (complex R)
   double* trace_z;      // trace z values, instance slots start at InstDev::tracez_off
   long long max_attempts;  // attempts this launch may spend per instance (<=0: unbounded)
+  long long* prof;         // per-instance phase cycle counters (profiling builds only)
 };
 
 }  // namespace gnlse

@@ -28,8 +28,9 @@ class Instance:
     """One propagation: a field on grid ``grid`` through ``length`` km of fibre."""
 
     def __init__(self, grid, method="ark4ip", length=1.0, local_error=1e-6, total_steps=100,
-                 traces=1, max_traces=None, h0=0.0):
+                 traces=1, max_traces=None, h0=0.0, weight=0.0):
         self.grid = int(grid)
+        self.weight = float(weight)
         self.method = method.lower()
         if self.method not in METHODS:
             raise ValueError(f"unknown method {method!r} (rk4ip or ark4ip)")
@@ -91,6 +92,7 @@ class Plan:
             d.length = s.length
             d.local_error = s.local_error
             d.h0 = s.h0
+            d.weight = s.weight
         handle = ct.c_void_p()
         with torch.cuda.device(self.device):
             nat.check(lib.gnlse_plan_create(PRECISIONS[precision], len(self.grids), gd,

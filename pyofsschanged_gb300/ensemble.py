@@ -81,9 +81,21 @@ def ensemble_plan_inputs(members, domains, local_error=1e-6, cluster=None):
     cluster = cluster or {}
     grids = [GridTables(domains[n], cluster=cluster.get(n, 0), **FIBRE_835) for n in sizes]
     index = {n: i for i, n in enumerate(sizes)}
-    inst = [Instance(index[m.n], method="ark4ip", length=m.length, local_error=local_error)
-            for m in members]
+    inst = [Instance(index[m.n], method="ark4ip", length=m.length, local_error=local_error,
+                     weight=expected_attempts(m)) for m in members]
     return grids, inst
+
+
+def expected_attempts(m):
+    """Relative ARK4IP work of a member: attempts grow as L sqrt(P0 T0).
+
+    Step doubling keeps the nonlinear phase per step roughly constant, and the
+    spectral bandwidth the steps must resolve grows with the soliton order
+    N = sqrt(gamma P0 T0^2 / |beta2|); fitting the FP64 oracle's attempt counts
+    of the benchmark ensemble gives exponents (1.01, 0.51, 0.46) for (L, P0, T0).
+    """
+    t0 = m.fwhm / (2.0 * math.log(1.0 + math.sqrt(2.0)))
+    return m.length * math.sqrt(m.peak_power * t0)
 
 
 def coherence_g12(spectra):
