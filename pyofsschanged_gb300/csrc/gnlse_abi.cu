@@ -318,12 +318,12 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     // 4096 (complex128: one CTA per SM); larger grids span a cluster
     const int mmax = 4096;
     if (C == 0) {
-      // Measured per-transform cost (GB300, complex64): the cross-CTA exchange
-      // through distributed shared memory costs more per byte than the local
-      // passes, so a 2^14 field runs fastest as 8 CTAs x 2048 points (4.5 us
-      // per transform) rather than 4 x 4096 (9.2 us); 2^13 as 2 x 4096.
+      // Measured on GB300 (mixed precision, SM time per attempt with the GPU
+      // saturated): a 2^14 field costs 1550 / 1470 / 1560 us as 2 / 4 / 8 CTAs,
+      // so 4096 points per CTA is kept; a single 8192-point CTA would use less
+      // SM time than two of 4096 (546 vs 622 us) but doubles the attempt
+      // latency, which bounds the longest propagations of an ensemble.
       C = n <= mmax ? 1 : n / mmax;
-      if (precision != GNLSE_FP64 && n == 4 * mmax) C = 8;
       if (C > 8) C = n / (2 * mmax);  // complex64 2^16: 8 CTAs of 8192 points
     }
     if (C != 1 && C != 2 && C != 4 && C != 8) {

@@ -28,8 +28,13 @@
 #include "gnlse_twiddle.h"
 #include "gnlse_types.h"
 
+// registers per thread the launch bounds aim for: CTAs per SM = 65536 / (T * this),
+// limited by shared memory (GNLSE_MINB_CAP can lower it further)
+#ifndef GNLSE_REGS_TARGET
+#define GNLSE_REGS_TARGET 128
+#endif
 #ifndef GNLSE_MINB_CAP
-#define GNLSE_MINB_CAP 2
+#define GNLSE_MINB_CAP 16
 #endif
 #ifndef GNLSE_RAMAN_SPLIT
 #define GNLSE_RAMAN_SPLIT 0
@@ -168,9 +173,11 @@ struct Engine {
   // CTAs that fit on one SM by shared memory (228 KB per SM, 1 KB reserved per CTA)
   static constexpr int NBUF = (C > 1 && !INPLACE) ? 3 : 2;  // X, P (+ W)
   static constexpr int MINB_RAW = (int)(233472 / (NBUF * MP * sizeof(V) + RED * sizeof(double) + 1024 + 1024));
-  // ... capped so that a thread keeps at least 64 registers (and at most
-  // GNLSE_MINB_CAP CTAs per SM are assumed when allocating registers)
-  static constexpr int MINB_REG = MINB_RAW < 1 ? 1 : (MINB_RAW * T > 1024 ? 1024 / T : MINB_RAW);
+  // ... and by the register target (128 registers: 2 CTAs of 256 threads, 4 of 128;
+  // 64-thread CTAs of the small grids keep up to 255)
+  static constexpr int TR = T < 128 ? 128 : T;
+  static constexpr int MINB_TGT = 65536 / (TR * GNLSE_REGS_TARGET) < 1 ? 1 : 65536 / (TR * GNLSE_REGS_TARGET);
+  static constexpr int MINB_REG = MINB_RAW < 1 ? 1 : (MINB_RAW < MINB_TGT ? MINB_RAW : MINB_TGT);
   static constexpr int MINB = MINB_REG < GNLSE_MINB_CAP ? MINB_REG : GNLSE_MINB_CAP;
   static constexpr size_t smem_bytes() {
     return NBUF * MP * sizeof(V) + RED * sizeof(double) + ctl_bytes();
@@ -187,9 +194,15 @@ struct Engine {
     int rank;
   };
 
+  // Address of p's counterpart in CTA r of the cluster.  The mapping is an
+  // opaque (volatile) instruction at every use, so the compiler recomputes it
+  // instead of keeping the C remote bases of every buffer live across the
+  // whole propagation loop (which spilled registers in the cluster classes).
   static __device__ __forceinline__ V* rmt(V* p, int r) {
     if constexpr (C > 1) {
-      return cg::this_cluster().map_shared_rank(p, r);
+      unsigned long long q;
+      asm volatile("mapa.u64 %0, %1, %2;" : "=l"(q) : "l"(p), "r"(r));
+      return reinterpret_cast<V*>(q);
     } else {
       return p;
     }
@@ -203,8 +216,11 @@ struct Engine {
     }
   }
 
+  // Twiddles are read with ordinary (L1-cached) loads rather than __ldg: the
+  // non-coherent loads may be hoisted across the barriers into earlier
+  // passes, which lengthens register lifetimes until the kernel spills.
   static __device__ __forceinline__ V twid(const V* tw, int idx, int sign) {
-    V w = __ldg(&tw[idx]);
+    V w = tw[idx];
     if (sign < 0) w.y = -w.y;
     return w;
   }
@@ -219,13 +235,13 @@ struct Engine {
     if constexpr (sizeof(V) == 8) {
 #pragma unroll
       for (int i = 0; i < RAD / 2; ++i) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(row) + i);
+        const float4 q = *(reinterpret_cast<const float4*>(row) + i);
         w[2 * i] = mk<V>(q.x, q.y);
         w[2 * i + 1] = mk<V>(q.z, q.w);
       }
     } else {
 #pragma unroll
-      for (int r = 0; r < RAD; ++r) w[r] = __ldg(row + r);
+      for (int r = 0; r < RAD; ++r) w[r] = row[r];
     }
   }
 
@@ -502,10 +518,6 @@ struct Engine {
     if (op.gain) e = cscale(e, (R)exp(ga * __ldg(&op.lor[a])));
     return e;
   }
-  static __device__ __forceinline__ V hK(const Op& op, int a, V v) {  // h * i * K * v
-    const R k = op.h * __ldg(&op.Kr[a]);
-    return mk<V>(-k * v.y, k * v.x);
-  }
   // complex64 value (or the leading part of a double-float value) of a state-like array
   static __device__ __forceinline__ V ldv(const SV* p, int a) {
     if constexpr (XS) {
@@ -725,11 +737,45 @@ struct Engine {
   }
 
   // ---- elementwise stage loops (fused end of one stage / start of the next) --
+  // Each loop visits this CTA's M slots in batches of U per thread: every load
+  // of a batch (global state arrays and the shared X slot) is issued before
+  // the batch's arithmetic and stores, so U slots' loads are in flight at once.
+  // (Loads cannot be hoisted above the previous slot's stores by the compiler,
+  // which must assume they may alias.)  M is a multiple of 4 T for every class.
+  using SL = typename std::conditional<XS, dfc, V>::type;  // full-precision state value
+  static __device__ __forceinline__ SL lds(const SV* p, int a) {
+    if constexpr (XS) {
+      return dfc_load(p, a);
+    } else {
+      return p[a];
+    }
+  }
+  static __device__ __forceinline__ V slhi(const SL& v) {
+    if constexpr (XS) {
+      return dfc_hi(v);
+    } else {
+      return v;
+    }
+  }
+  static __device__ __forceinline__ V ik(R k, V v) { return mk<V>(-k * v.y, k * v.x); }  // i k v
+
+  template <int U, class In, class Ld, class St>
+  static __device__ __forceinline__ void each_slot(Ld&& ld, St&& st) {
+    static_assert(M % (U * T) == 0, "slot batches must tile the slice");
+    for (int l0 = threadIdx.x; l0 < M; l0 += U * T) {
+      In in[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) in[u] = ld(l0 + u * T);
+#pragma unroll
+      for (int u = 0; u < U; ++u) st(l0 + u * T, in[u]);
+    }
+  }
+
   // X = Z (stage input of N(A) for state Z)
   static __device__ __forceinline__ void load_state(const Ctx& cx, const SV* Z) {
     const int base = cx.rank * M;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) cx.X[pad(l)] = ldv(Z, base + l);
+    V* X = cx.X;
+    each_slot<4, V>([&](int l) { return ldv(Z, base + l); }, [&](int l, const V& v) { X[pad(l)] = v; });
     __syncthreads();
   }
 
@@ -737,72 +783,87 @@ struct Engine {
   static __device__ __forceinline__ void store_ma(const Ctx& cx, const GridDev& g, V* MA) {
     const R* Kr = (const R*)g.Kr;
     const int base = cx.rank * M;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) {
-      const V v = cx.X[pad(l)];
-      const R k = __ldg(&Kr[base + l]);
-      MA[base + l] = mk<V>(-k * v.y, k * v.x);
-    }
+    V* X = cx.X;
+    struct In { V x; R k; };
+    each_slot<4, In>([&](int l) { return In{X[pad(l)], __ldg(&Kr[base + l])}; },
+                     [&](int l, const In& r) { MA[base + l] = ik(r.k, r.x); });
     __syncthreads();
   }
 
   // stage 1 input: S_I + k0/2 with S_I = L(A), k0 = L(h N(A))
-  static __device__ __forceinline__ void pre_stage1(const Ctx& cx, const Op& op) {
+  static __device__ __forceinline__ void pre_stage1(const Ctx& cx, const Op& ops) {
+    const Op op = ops;
     const R half = (R)0.5;
     const int base = cx.rank * M;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) {
-      const int a = base + l;
-      const V e = ldv(op.Et, a);
-      const V si = cmul(mult(op, a, e, op.aA), ldv(op.S0, a));
-      const V k0 = cscale(cmul(mult(op, a, e, op.ak0), op.MA0[a]), op.h);
-      cx.X[pad(l)] = cadd(si, cscale(k0, half));
-    }
+    V* X = cx.X;
+    struct In { V e, s0, ma; };
+    each_slot<4, In>(
+        [&](int l) {
+          const int a = base + l;
+          return In{ldv(op.Et, a), ldv(op.S0, a), op.MA0[a]};
+        },
+        [&](int l, const In& r) {
+          const int a = base + l;
+          const V si = cmul(mult(op, a, r.e, op.aA), r.s0);
+          const V k0 = cscale(cmul(mult(op, a, r.e, op.ak0), r.ma), op.h);
+          X[pad(l)] = cadd(si, cscale(k0, half));
+        });
     __syncthreads();
   }
 
   // k1 = h N; acc = S_I + k0/6 + k1/3; stage 2 input S_I + k1/2
-  static __device__ __forceinline__ void post_stage1(const Ctx& cx, const Op& op) {
+  static __device__ __forceinline__ void post_stage1(const Ctx& cx, const Op& ops) {
+    const Op op = ops;
     const R half = (R)0.5, sixth = (R)(1.0 / 6.0), third = (R)(1.0 / 3.0);
     const int base = cx.rank * M;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) {
-      const int a = base + l;
-      const V k1 = hK(op, a, cx.X[pad(l)]);
-      if constexpr (XS) {
-        const dfc e = dfc_load(op.Et, a);
-        const dfc si = dfc_mul(mult_df(op, a, e, op.aA), dfc_load(op.S0, a));
-        const V k0 = cscale(cmul(mult(op, a, dfc_hi(e), op.ak0), op.MA0[a]), op.h);
-        dfc_store(op.acc, a, dfc_add_f(si, cadd(cscale(k0, sixth), cscale(k1, third))));
-        cx.X[pad(l)] = cadd(dfc_hi(si), cscale(k1, half));
-      } else {
-        const V e = op.Et[a];
-        const V si = cmul(mult(op, a, e, op.aA), op.S0[a]);
-        const V k0 = cscale(cmul(mult(op, a, e, op.ak0), op.MA0[a]), op.h);
-        op.acc[a] = cadd(cadd(si, cscale(k0, sixth)), cscale(k1, third));
-        cx.X[pad(l)] = cadd(si, cscale(k1, half));
-      }
-    }
+    V* X = cx.X;
+    struct In { V x; R k; SL e, s0; V ma; };
+    each_slot<4, In>(
+        [&](int l) {
+          const int a = base + l;
+          return In{X[pad(l)], __ldg(&op.Kr[a]), lds(op.Et, a), lds(op.S0, a), op.MA0[a]};
+        },
+        [&](int l, const In& r) {
+          const int a = base + l;
+          const V k1 = ik(op.h * r.k, r.x);
+          if constexpr (XS) {
+            const dfc si = dfc_mul(mult_df(op, a, r.e, op.aA), r.s0);
+            const V k0 = cscale(cmul(mult(op, a, dfc_hi(r.e), op.ak0), r.ma), op.h);
+            dfc_store(op.acc, a, dfc_add_f(si, cadd(cscale(k0, sixth), cscale(k1, third))));
+            X[pad(l)] = cadd(dfc_hi(si), cscale(k1, half));
+          } else {
+            const V si = cmul(mult(op, a, r.e, op.aA), r.s0);
+            const V k0 = cscale(cmul(mult(op, a, r.e, op.ak0), r.ma), op.h);
+            op.acc[a] = cadd(cadd(si, cscale(k0, sixth)), cscale(k1, third));
+            X[pad(l)] = cadd(si, cscale(k1, half));
+          }
+        });
     __syncthreads();
   }
 
   // k2 = h N; acc += k2/3; stage 3 input L(S_I + k2) (gain: S_I + k2, scaled after)
-  static __device__ __forceinline__ void post_stage2(const Ctx& cx, const Op& op) {
+  static __device__ __forceinline__ void post_stage2(const Ctx& cx, const Op& ops) {
+    const Op op = ops;
     const R third = (R)(1.0 / 3.0);
     const int base = cx.rank * M;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) {
-      const int a = base + l;
-      const V k2 = hK(op, a, cx.X[pad(l)]);
-      if constexpr (XS) {
-        dfc_store(op.acc, a, dfc_add_f(dfc_load(op.acc, a), cscale(k2, third)));
-      } else {
-        op.acc[a] = cadd(op.acc[a], cscale(k2, third));
-      }
-      const V e = ldv(op.Et, a);
-      const V u = cadd(cmul(mult(op, a, e, op.aA), ldv(op.S0, a)), k2);
-      cx.X[pad(l)] = op.gain ? u : cmul(e, u);
-    }
+    V* X = cx.X;
+    struct In { V x; R k; SL acc; V e, s0; };
+    each_slot<4, In>(
+        [&](int l) {
+          const int a = base + l;
+          return In{X[pad(l)], __ldg(&op.Kr[a]), lds(op.acc, a), ldv(op.Et, a), ldv(op.S0, a)};
+        },
+        [&](int l, const In& r) {
+          const int a = base + l;
+          const V k2 = ik(op.h * r.k, r.x);
+          if constexpr (XS) {
+            dfc_store(op.acc, a, dfc_add_f(r.acc, cscale(k2, third)));
+          } else {
+            op.acc[a] = cadd(r.acc, cscale(k2, third));
+          }
+          const V u = cadd(cmul(mult(op, a, r.e, op.aA), r.s0), k2);
+          X[pad(l)] = op.gain ? u : cmul(r.e, u);
+        });
     __syncthreads();
   }
 
@@ -817,46 +878,58 @@ struct Engine {
 
   // k3 = h N; result = L(acc) + k3/6 -> out; coarse: error norms against Sf and
   // the local extrapolation (stepper.py:272-274,338) (16 A_fine - A_coarse)/15 -> out.
-  static __device__ __forceinline__ void post_stage3(const Ctx& cx, const Op& op, bool coarse,
+  static __device__ __forceinline__ void post_stage3(const Ctx& cx, const Op& ops, bool coarse,
                                                      double (&s)[3]) {
+    const Op op = ops;
     const R sixth = (R)(1.0 / 6.0);
     const R fa = (R)(16.0 / 15.0), fb = (R)(1.0 / 15.0);
     const int base = cx.rank * M;
+    V* X = cx.X;
     R d2 = 0, f2 = 0;
     double bad = 0.0;
-#pragma unroll 4
-    for (int l = threadIdx.x; l < M; l += T) {
-      const int a = base + l;
-      const V k3 = hK(op, a, cx.X[pad(l)]);
-      if constexpr (XS) {
-        const dfc res = dfc_add_f(dfc_mul(mult_df(op, a, dfc_load(op.Et, a), op.ao), dfc_load(op.acc, a)),
-                                  cscale(k3, sixth));
-        if (!coarse) {
-          dfc_store(op.out, a, res);
-        } else {
-          const dfc sf = dfc_load(op.Sf, a);
-          const dfc d = dfc_sub(sf, res);
-          d2 += d.re.hi * d.re.hi + d.im.hi * d.im.hi;
-          f2 += sf.re.hi * sf.re.hi + sf.im.hi * sf.im.hi;
-          if (!isfinite(sf.re.hi) || !isfinite(sf.im.hi)) bad = 1.0;
-          const dff FA = {(float)(16.0 / 15.0), (float)(16.0 / 15.0 - (double)(float)(16.0 / 15.0))};
-          const dff FB = {(float)(-1.0 / 15.0), (float)(-1.0 / 15.0 - (double)(float)(-1.0 / 15.0))};
-          dfc_store(op.out, a, dfc_add(dfc_scale(sf, FA), dfc_scale(res, FB)));
-        }
-      } else {
-        const V res = cadd(cmul(mult(op, a, op.Et[a], op.ao), op.acc[a]), cscale(k3, sixth));
-        if (!coarse) {
-          op.out[a] = res;
-        } else {
-          const V sf = op.Sf[a];
-          const V d = csub(sf, res);
-          d2 += cabs2(d);
-          f2 += cabs2(sf);
-          if (!isfinite(sf.x) || !isfinite(sf.y)) bad = 1.0;
-          op.out[a] = mk<V>(fa * sf.x - fb * res.x, fa * sf.y - fb * res.y);
-        }
-      }
-    }
+    struct In { V x; R k; SL e, acc, sf; };
+    each_slot<4, In>(
+        [&](int l) {
+          const int a = base + l;
+          In r;
+          r.x = X[pad(l)];
+          r.k = __ldg(&op.Kr[a]);
+          r.e = lds(op.Et, a);
+          r.acc = lds(op.acc, a);
+          if (coarse) r.sf = lds(op.Sf, a);
+          return r;
+        },
+        [&](int l, const In& r) {
+          const int a = base + l;
+          const V k3 = ik(op.h * r.k, r.x);
+          if constexpr (XS) {
+            const dfc res = dfc_add_f(dfc_mul(mult_df(op, a, r.e, op.ao), r.acc), cscale(k3, sixth));
+            if (!coarse) {
+              dfc_store(op.out, a, res);
+            } else {
+              const dfc sf = r.sf;
+              const dfc d = dfc_sub(sf, res);
+              d2 += d.re.hi * d.re.hi + d.im.hi * d.im.hi;
+              f2 += sf.re.hi * sf.re.hi + sf.im.hi * sf.im.hi;
+              if (!isfinite(sf.re.hi) || !isfinite(sf.im.hi)) bad = 1.0;
+              const dff FA = {(float)(16.0 / 15.0), (float)(16.0 / 15.0 - (double)(float)(16.0 / 15.0))};
+              const dff FB = {(float)(-1.0 / 15.0), (float)(-1.0 / 15.0 - (double)(float)(-1.0 / 15.0))};
+              dfc_store(op.out, a, dfc_add(dfc_scale(sf, FA), dfc_scale(res, FB)));
+            }
+          } else {
+            const V res = cadd(cmul(mult(op, a, r.e, op.ao), r.acc), cscale(k3, sixth));
+            if (!coarse) {
+              op.out[a] = res;
+            } else {
+              const V sf = r.sf;
+              const V d = csub(sf, res);
+              d2 += cabs2(d);
+              f2 += cabs2(sf);
+              if (!isfinite(sf.x) || !isfinite(sf.y)) bad = 1.0;
+              op.out[a] = mk<V>(fa * sf.x - fb * res.x, fa * sf.y - fb * res.y);
+            }
+          }
+        });
     s[0] = d2;
     s[1] = f2;
     s[2] = bad;

@@ -16,7 +16,8 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
 #define GNLSE_CLASSES_F32(X) X(float, 12, 1)
 #define GNLSE_CLASSES_F64(X)
 #define GNLSE_CLASSES_MIX(X) \
-  X(float, 12, 1) X(float, 12, 2) X(float, 12, 4) X(float, 11, 2) X(float, 11, 4) X(float, 11, 8)
+  X(float, 12, 1) X(float, 12, 2) X(float, 12, 4) X(float, 11, 2) X(float, 11, 4) X(float, 11, 8) \
+  X(float, 13, 1) X(float, 13, 2)
 #else
 #define GNLSE_CLASSES_F32(X) \
   X(float, 8, 1) X(float, 9, 1) X(float, 10, 1) X(float, 11, 1) X(float, 12, 1) X(float, 13, 1) \
@@ -30,7 +31,7 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
 #define GNLSE_CLASSES_MIX(X) \
   X(float, 8, 1) X(float, 9, 1) X(float, 10, 1) X(float, 11, 1) X(float, 12, 1) \
   X(float, 9, 2) X(float, 12, 2) X(float, 8, 4) X(float, 12, 4) X(float, 12, 8) X(float, 13, 8) \
-  X(float, 11, 2) X(float, 11, 4) X(float, 11, 8)
+  X(float, 11, 2) X(float, 11, 4) X(float, 11, 8) X(float, 13, 1) X(float, 13, 2)
 #endif
 
 }  // namespace gnlse
