@@ -27,19 +27,18 @@ struct ClassRun {
   int level;  // 0 = longest predicted propagations (highest stream priority)
 };
 
-// Predicted per-attempt latency (relative units) of a field in class (logm, C):
-// measured GB300 transform times per cluster, 44 transforms per attempt.
-double attempt_cost(int logm, int C, int precision) {
-  const int M = 1 << logm;
-  double t;
-  if (logm == 12 && C == 1) t = 2.2;
-  else if (logm == 12 && C == 2) t = 4.0;
-  else if (logm == 12 && C == 4) t = 9.2;
-  else if (logm == 11 && C == 2) t = 2.3;
-  else if (logm == 11 && C == 4) t = 4.0;
-  else if (logm == 11 && C == 8) t = 4.5;
-  else t = 2.2 * (M / 4096.0) * (logm / 12.0) * (C > 1 ? 1.0 + 0.5 * std::log2((double)C) : 1.0);
-  return precision == GNLSE_FP64 ? 30.0 * t : t;
+// SM time (us) of one attempt of one field in class (logm, C), measured on
+// GB300 in mixed precision with the GPU saturated by fields of that class;
+// only ratios between classes are used.  Other classes: n log n scaling of the
+// 4096-point single-CTA figure, plus half again for a cluster exchange.
+double sm_cost(int logm, int C) {
+  struct Entry { int logm, C; double us; };
+  static const Entry tab[] = {{12, 1, 190.5}, {11, 2, 259.6},  {13, 1, 495.2},  {12, 2, 588.9},
+                              {11, 4, 565.4}, {13, 2, 1496.0}, {12, 4, 1383.1}, {11, 8, 1331.4}};
+  for (const Entry& e : tab)
+    if (e.logm == logm && e.C == C) return e.us;
+  const double n = (double)(1 << logm) * C;
+  return 190.5 * (n / 4096.0) * (std::log2(n) / 12.0) * (C > 1 ? 1.5 : 1.0);
 }
 
 struct GridHost {
@@ -303,8 +302,9 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   p->vsize = precision == GNLSE_FP32 ? 8 : 16;
   p->ssize = precision == GNLSE_FP32 ? 8 : 16;
   cudaGetDevice(&p->device);
-  std::vector<GridDev> gdev(n_grids);
-  p->grids.resize(n_grids);
+  // ---- grids: validation and the cluster sizes each may run with -------------
+  std::vector<std::vector<int>> cands(n_grids);  // candidate cluster sizes, fixed or auto
+  std::vector<int> tput(n_grids), lat(n_grids);   // throughput / latency choice (auto grids)
   for (int i = 0; i < n_grids; ++i) {
     const gnlse_grid_desc& gd = grids[i];
     const int n = gd.n;
@@ -313,40 +313,52 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
-    int C = gd.cluster;
-    // points per CTA: 4096 (complex64: 3 CTAs of 256 threads fit one SM) or
-    // 4096 (complex128: one CTA per SM); larger grids span a cluster
-    const int mmax = 4096;
-    if (C == 0) {
-      // Measured on GB300 (mixed precision, SM time per attempt with the GPU
-      // saturated): a 2^14 field costs 1550 / 1470 / 1560 us as 2 / 4 / 8 CTAs,
-      // so 4096 points per CTA is kept; a single 8192-point CTA would use less
-      // SM time than two of 4096 (546 vs 622 us) but doubles the attempt
-      // latency, which bounds the longest propagations of an ensemble.
-      C = n <= mmax ? 1 : n / mmax;
-      if (C > 8) C = n / (2 * mmax);  // complex64 2^16: 8 CTAs of 8192 points
+    if (gd.cluster != 0) {
+      const int C = gd.cluster;
+      if ((C != 1 && C != 2 && C != 4 && C != 8) || n % C != 0 || !supported(precision, ilog2i(n / C), C)) {
+        free_plan(p);
+        return GNLSE_UNSUPPORTED;
+      }
+      tput[i] = lat[i] = C;
+      continue;
     }
-    if (C != 1 && C != 2 && C != 4 && C != 8) {
+    if (precision == GNLSE_FP64) {
+      // complex128: 4096 points per CTA (one CTA per SM), larger grids span a cluster
+      const int C = n <= 4096 ? 1 : n / 4096;
+      if (C > 8 || !supported(precision, ilog2i(n / C), C)) {
+        free_plan(p);
+        return GNLSE_UNSUPPORTED;
+      }
+      tput[i] = lat[i] = C;
+      continue;
+    }
+    // complex64 transforms: the cheapest class in SM time, and the class with the
+    // least SM time per CTA (attempt latency) among those within 1.5x of it.
+    // Slices of up to 4096 points per CTA only (8192-point CTAs fill an SM on
+    // their own and pack badly beside the other classes of an ensemble),
+    // except for grids above 8 x 4096 points.
+    const int mcap = n > 8 * 4096 ? 13 : 12;
+    int best = 0, fast = 0;
+    for (int C = 1; C <= 8; C *= 2) {
+      const int logm = ilog2i(n / C);
+      if (n / C < 256 || logm > mcap || !supported(precision, logm, C)) continue;
+      if (!best || sm_cost(logm, C) < sm_cost(ilog2i(n / best), best)) best = C;
+    }
+    if (!best) {
       free_plan(p);
       return GNLSE_UNSUPPORTED;
     }
-    const int logm = ilog2i(n / C);
-    if (n % C != 0 || !supported(precision, logm, C)) {
-      free_plan(p);
-      return GNLSE_UNSUPPORTED;
+    const double cb = sm_cost(ilog2i(n / best), best);
+    for (int C = 1; C <= 8; C *= 2) {
+      const int logm = ilog2i(n / C);
+      if (n / C < 256 || logm > mcap || !supported(precision, logm, C) || sm_cost(logm, C) > 1.5 * cb) continue;
+      if (!fast || sm_cost(logm, C) / C < sm_cost(ilog2i(n / fast), fast) / fast) fast = C;
     }
-    GridHost& gh = p->grids[i];
-    gh.n = n;
-    gh.logm = logm;
-    gh.C = C;
-    cudaError_t e = precision == GNLSE_FP64
-                        ? build_grid_tables<double>(p, gd, gh, gdev[i], false)
-                        : build_grid_tables<float>(p, gd, gh, gdev[i], precision == GNLSE_MIXED);
-    if (e != cudaSuccess) {
-      free_plan(p);
-      return cuda_fail(e);
-    }
+    tput[i] = best;
+    lat[i] = fast;
   }
+
+  // ---- instances -------------------------------------------------------------
   p->inst.resize(n_instances);
   p->field_off.resize(n_instances);
   p->trace_off.resize(n_instances);
@@ -360,7 +372,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
-    const int n = p->grids[id.grid].n;
+    const int n = grids[id.grid].n;
     InstDev& d = p->inst[i];
     memset(&d, 0, sizeof(d));
     d.grid = id.grid;
@@ -392,23 +404,95 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   p->trace_elems = toff;
   p->tracez_elems = zoff;
   p->scratch_bytes = (size_t)soff * p->ssize;
-  // Launch schedule: predicted duration = work weight x per-attempt cost of the
-  // instance's class.  Instances whose predicted duration is within 60% of the
-  // longest start at level 0, down to 30% at level 1, the rest at level 2; each
-  // (level, class) pair is one launch, and levels map to decreasing stream
-  // priorities, so long propagations of every grid size get SMs first
-  // (longest-processing-time-first across the launches).
+
+  // ---- class of each instance and launch schedule -----------------------------
+  // Work w_i = the caller's weight (expected attempts) or the fibre length.
+  // Every instance starts in its grid's cheapest class; the makespan is about
+  // max(total SM time / SMs, longest chain), with a chain's time ~ 3 w_i x SM
+  // time per attempt / C (about three CTAs share an SM when the GPU is full).
+  // Instances whose chain exceeds the work bound move, longest first, to the
+  // lower-latency class of their grid while that still shortens the longest chain.
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+  if (nsm <= 0) nsm = 1;
+  std::vector<int> icl(n_instances);
+  std::vector<double> w(n_instances);
+  auto icost = [&](int i, int C) { return sm_cost(ilog2i(grids[instances[i].grid].n / C), C); };
+  auto chain = [&](int i, int C) { return 3.0 * w[i] * icost(i, C) / C; };
+  double work = 0.0;
+  for (int i = 0; i < n_instances; ++i) {
+    w[i] = instances[i].weight > 0 ? instances[i].weight : (p->inst[i].length > 0 ? p->inst[i].length : 1.0);
+    icl[i] = tput[instances[i].grid];
+    work += w[i] * icost(i, icl[i]) / nsm;
+  }
   std::vector<int> ids(n_instances);
+  for (int i = 0; i < n_instances; ++i) ids[i] = i;
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return chain(a, icl[a]) > chain(b, icl[b]); });
+  for (int i : ids) {
+    const int L = lat[instances[i].grid];
+    if (chain(i, icl[i]) <= work) break;
+    if (L == icl[i] || chain(i, L) >= chain(i, icl[i])) continue;
+    work += w[i] * (icost(i, L) - icost(i, icl[i])) / nsm;
+    icl[i] = L;
+  }
+  // device tables for every (grid, cluster size) pair in use
+  std::vector<GridDev> gdev;
+  std::vector<int> vgrid, vC;
+  for (int i = 0; i < n_instances; ++i) {
+    const int g = instances[i].grid;
+    int v = 0;
+    while (v < (int)vgrid.size() && !(vgrid[v] == g && vC[v] == icl[i])) ++v;
+    if (v == (int)vgrid.size()) {
+      vgrid.push_back(g);
+      vC.push_back(icl[i]);
+    }
+    p->inst[i].grid = v;
+  }
+  p->grids.resize(vgrid.size());
+  gdev.resize(vgrid.size());
+  for (size_t v = 0; v < vgrid.size(); ++v) {
+    const gnlse_grid_desc& gd = grids[vgrid[v]];
+    GridHost& gh = p->grids[v];
+    gh.n = gd.n;
+    gh.C = vC[v];
+    gh.logm = ilog2i(gd.n / gh.C);
+    cudaError_t e = precision == GNLSE_FP64
+                        ? build_grid_tables<double>(p, gd, gh, gdev[v], false)
+                        : build_grid_tables<float>(p, gd, gh, gdev[v], precision == GNLSE_MIXED);
+    if (e != cudaSuccess) {
+      free_plan(p);
+      return cuda_fail(e);
+    }
+  }
+  // Launches: each (level, class) pair is one launch on its own stream, and
+  // levels map to decreasing stream priorities, so long propagations of every
+  // grid size get SMs first.  With three levels, instances whose chain is
+  // within 60% of the longest start at level 0, down to 30% at level 1;
+  // with two, the split is at 50%.  Levels are limited so that the launches
+  // need at most 8 streams: the device multiplexes streams onto 8 hardware
+  // queues by default, and a launch sharing a queue waits behind the other.
   std::vector<double> dur(n_instances);
   double dmax = 0.0;
   for (int i = 0; i < n_instances; ++i) {
-    ids[i] = i;
-    const GridHost& g = p->grids[p->inst[i].grid];
-    const double w = instances[i].weight > 0 ? instances[i].weight : p->inst[i].length;
-    dur[i] = w * attempt_cost(g.logm, g.C, precision);
+    dur[i] = chain(i, icl[i]);
     dmax = std::max(dmax, dur[i]);
   }
-  auto level = [&](int i) { return dur[i] >= 0.6 * dmax ? 0 : (dur[i] >= 0.3 * dmax ? 1 : 2); };
+  int nclass = 0;
+  {
+    std::vector<int> seen;
+    for (int i = 0; i < n_instances; ++i) {
+      const GridHost& g = p->grids[p->inst[i].grid];
+      const int k = g.logm * 16 + g.C;
+      if (std::find(seen.begin(), seen.end(), k) == seen.end()) seen.push_back(k);
+    }
+    nclass = (int)seen.size();
+  }
+  const int nlevels = std::max(1, std::min(3, 8 / std::max(1, nclass)));
+  auto level = [&](int i) {
+    if (nlevels == 3) return dur[i] >= 0.6 * dmax ? 0 : (dur[i] >= 0.3 * dmax ? 1 : 2);
+    if (nlevels == 2) return dur[i] >= 0.5 * dmax ? 0 : 1;
+    return 0;
+  };
   auto cls = [&](int i) { const GridHost& g = p->grids[p->inst[i].grid]; return g.logm * 16 + g.C; };
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) {
     if (level(a) != level(b)) return level(a) < level(b);

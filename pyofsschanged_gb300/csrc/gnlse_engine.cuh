@@ -83,6 +83,25 @@ template <class V> __device__ __forceinline__ auto cabs2(V a) -> decltype(a.x) {
 // 16-byte elements.
 __device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
 
+// threadIdx.x read through an opaque instruction: index arithmetic derived from
+// it is recomputed where it is used instead of being hoisted out of the
+// propagation loop and kept live in registers across every transform.
+// GNLSE_OPAQUE_TID selects where: bit 0 Stockham passes, bit 1 cross-CTA
+// passes, bit 2 elementwise stage loops.
+#ifndef GNLSE_OPAQUE_TID
+#define GNLSE_OPAQUE_TID 1
+#endif
+template <int BIT>
+__device__ __forceinline__ int tidx() {
+  if constexpr ((GNLSE_OPAQUE_TID >> BIT) & 1) {
+    int t;
+    asm volatile("mov.u32 %0, %%tid.x;" : "=r"(t));
+    return t;
+  } else {
+    return (int)threadIdx.x;
+  }
+}
+
 __host__ __device__ constexpr int bitrev(int k, int bits) {
   int r = 0;
   for (int b = 0; b < bits; ++b) r |= ((k >> b) & 1) << (bits - 1 - b);
@@ -251,7 +270,7 @@ struct Engine {
     constexpr int NB = M / RAD;
     constexpr int BPT = (NB + T - 1) / T;
     V v[BPT][RAD];
-    const int tid = threadIdx.x;
+    const int tid = tidx<0>();
 #pragma unroll
     for (int b = 0; b < BPT; ++b) {
       const int j = tid + b * T;
@@ -318,6 +337,7 @@ struct Engine {
   template <class Pro>
   static __device__ __forceinline__ void cross_fwd(const Ctx& cx, Pro& pro, bool lead) {
     constexpr int PM = M / C;
+    const int tid = tidx<1>();
     if constexpr (INPLACE) {
       // in place: all reads, cluster barrier, all writes (into cx.W == cx.X)
       constexpr int BP = (PM + T - 1) / T;
@@ -325,7 +345,7 @@ struct Engine {
       csync();
 #pragma unroll
       for (int b = 0; b < BP; ++b) {
-        const int q = threadIdx.x + b * T;
+        const int q = tid + b * T;
         if (PM % T == 0 || q < PM)
 #pragma unroll
           for (int r = 0; r < C; ++r) v[b][r] = pro(r, cx.rank * PM + q);
@@ -333,7 +353,7 @@ struct Engine {
       csync();
 #pragma unroll
       for (int b = 0; b < BP; ++b) {
-        const int q = threadIdx.x + b * T;
+        const int q = tid + b * T;
         if (PM % T == 0 || q < PM) {
           const int n2 = cx.rank * PM + q;
           dft<C, +1>(v[b]);
@@ -351,14 +371,14 @@ struct Engine {
     V v[BP][C];
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
+      const int q = tid + b * T;
       if (PM % T == 0 || q < PM)
 #pragma unroll
         for (int r = 0; r < C; ++r) v[b][r] = pro(r, cx.rank * PM + q);
     }
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
+      const int q = tid + b * T;
       if (PM % T == 0 || q < PM) {
         const int n2 = cx.rank * PM + q;
         dft<C, +1>(v[b]);
@@ -377,13 +397,14 @@ struct Engine {
   template <class Epi>
   static __device__ __forceinline__ void cross_inv(const Ctx& cx, Epi& epi) {
     constexpr int PM = M / C;
+    const int tid = tidx<1>();
     if constexpr (INPLACE) {
       constexpr int BP = (PM + T - 1) / T;
       V v[BP][C];
       csync();
 #pragma unroll
       for (int b = 0; b < BP; ++b) {
-        const int q = threadIdx.x + b * T;
+        const int q = tid + b * T;
         if (PM % T == 0 || q < PM)
 #pragma unroll
           for (int k1 = 0; k1 < C; ++k1) v[b][k1] = rmt(cx.W, k1)[pad(cx.rank * PM + q)];
@@ -391,7 +412,7 @@ struct Engine {
       csync();
 #pragma unroll
       for (int b = 0; b < BP; ++b) {
-        const int q = threadIdx.x + b * T;
+        const int q = tid + b * T;
         if (PM % T == 0 || q < PM) {
           const int n2 = cx.rank * PM + q;
 #pragma unroll
@@ -409,14 +430,14 @@ struct Engine {
     V v[BP][C];
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
+      const int q = tid + b * T;
       if (PM % T == 0 || q < PM)
 #pragma unroll
         for (int k1 = 0; k1 < C; ++k1) v[b][k1] = rmt(cx.W, k1)[pad(cx.rank * PM + q)];
     }
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
-      const int q = threadIdx.x + b * T;
+      const int q = tid + b * T;
       if (PM % T == 0 || q < PM) {
         const int n2 = cx.rank * PM + q;
 #pragma unroll
@@ -541,7 +562,14 @@ struct Engine {
   // |x|^2, on exit X holds G+(x R(x)) (spectral).  The transforms carry only
   // light per-element work in their first / last passes; with want_e the
   // Simpson energy (nJ) of x is returned.
+#ifndef GNLSE_NL_NOINLINE
+#define GNLSE_NL_NOINLINE 0
+#endif
+#if GNLSE_NL_NOINLINE
+  static __device__ __noinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
+#else
   static __device__ __forceinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
+#endif
     const R invN = (R)(1.0 / (double)N);
     const bool raman = g.raman != 0;
     V* X = cx.X;
@@ -762,7 +790,7 @@ struct Engine {
   template <int U, class In, class Ld, class St>
   static __device__ __forceinline__ void each_slot(Ld&& ld, St&& st) {
     static_assert(M % (U * T) == 0, "slot batches must tile the slice");
-    for (int l0 = threadIdx.x; l0 < M; l0 += U * T) {
+    for (int l0 = tidx<2>(); l0 < M; l0 += U * T) {
       In in[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) in[u] = ld(l0 + u * T);
