@@ -92,9 +92,26 @@ SIGNATURES = {
     "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
+    # spectral neural operator surrogate kernels (include/sno.h)
+    "sno_gemm": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                            ct.c_void_p, ct.c_longlong, ct.c_longlong,
+                            ct.c_void_p, ct.c_longlong, ct.c_longlong,
+                            ct.c_void_p, ct.c_longlong, ct.c_longlong, ct.c_int,
+                            ct.c_float, ct.c_float, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                            ct.c_longlong, ct.c_int, ct.c_void_p]),
+    "sno_gelu_backward": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                     ct.c_longlong, ct.c_void_p]),
+    "sno_to_bf16": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_longlong, ct.c_void_p]),
+    "sno_colsum": (ct.c_int, [ct.c_void_p, ct.c_longlong, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "sno_adam": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                            ct.c_longlong, ct.c_float, ct.c_float, ct.c_float, ct.c_float,
+                            ct.c_int, ct.c_float, ct.c_void_p]),
+    "sno_rel_l2": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_longlong, ct.c_int, ct.c_void_p,
+                              ct.c_void_p, ct.c_void_p]),
 }
 
-OPTIONAL = {"gnlse_propagate_noalloc"}
+OPTIONAL = {"gnlse_propagate_noalloc", "sno_gemm", "sno_gelu_backward", "sno_to_bf16", "sno_colsum",
+            "sno_adam", "sno_rel_l2"}
 
 _lib = None
 _lock = threading.Lock()

@@ -604,14 +604,17 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
   kp.max_attempts = max_attempts;
   kp.prof = p->d_prof;
   cudaError_t e;
+  // Timing events are recorded as external events, so that under stream capture
+  // they become event-record nodes of the graph and still time each replay
+  // (a plain record during capture only expresses a dependency).
   if (p->classes.size() == 1) {
     const ClassRun& c = p->classes[0];
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
-    if (p->timing && (e = cudaEventRecord(p->t0[0], s)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecordWithFlags(p->t0[0], s, cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
     e = dispatch(p->precision, c.logm, c.C, kp, c.count, s);
     if (e != cudaSuccess) return cuda_fail(e);
-    if (p->timing && (e = cudaEventRecord(p->t1[0], s)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecordWithFlags(p->t1[0], s, cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
     return GNLSE_OK;
   }
   // several classes: fork onto side streams so they share the GPU, then join
@@ -621,9 +624,9 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     if ((e = cudaStreamWaitEvent(p->side[k], p->fork, 0)) != cudaSuccess) return cuda_fail(e);
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
-    if (p->timing && (e = cudaEventRecord(p->t0[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecordWithFlags(p->t0[k], p->side[k], cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
     if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k])) != cudaSuccess) return cuda_fail(e);
-    if (p->timing && (e = cudaEventRecord(p->t1[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = cudaEventRecordWithFlags(p->t1[k], p->side[k], cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaEventRecord(p->ev[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaStreamWaitEvent(s, p->ev[k], 0)) != cudaSuccess) return cuda_fail(e);
   }

@@ -365,10 +365,19 @@ struct Engine {
       csync();
       return;
     }
-    if (lead) csync();
-    // all positions of a thread at once, so their remote loads overlap
+    // all positions of a thread at once, so their remote loads overlap; the
+    // twiddles W_N^{n2 k1} are requested before the barrier
     constexpr int BP = (PM + T - 1) / T;
     V v[BP][C];
+    V w[BP][C];
+#pragma unroll
+    for (int b = 0; b < BP; ++b) {
+      const int q = tid + b * T;
+      if (PM % T == 0 || q < PM)
+#pragma unroll
+        for (int k1 = 1; k1 < C; ++k1) w[b][k1] = twid(cx.tw, (cx.rank * PM + q) * k1, +1);
+    }
+    if (lead) csync();
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
       const int q = tid + b * T;
@@ -384,7 +393,7 @@ struct Engine {
         dft<C, +1>(v[b]);
 #pragma unroll
         for (int k1 = 0; k1 < C; ++k1) {
-          const V val = k1 ? cmul(v[b][k1], twid(cx.tw, n2 * k1, +1)) : v[b][k1];
+          const V val = k1 ? cmul(v[b][k1], w[b][k1]) : v[b][k1];
           rmt(cx.W, k1)[pad(n2)] = val;
         }
       }
@@ -425,9 +434,17 @@ struct Engine {
       csync();
       return;
     }
-    csync();
     constexpr int BP = (PM + T - 1) / T;
     V v[BP][C];
+    V w[BP][C];  // W_N^{-n2 k1}, requested before the barrier
+#pragma unroll
+    for (int b = 0; b < BP; ++b) {
+      const int q = tid + b * T;
+      if (PM % T == 0 || q < PM)
+#pragma unroll
+        for (int k1 = 1; k1 < C; ++k1) w[b][k1] = twid(cx.tw, (cx.rank * PM + q) * k1, -1);
+    }
+    csync();
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
       const int q = tid + b * T;
@@ -441,7 +458,7 @@ struct Engine {
       if (PM % T == 0 || q < PM) {
         const int n2 = cx.rank * PM + q;
 #pragma unroll
-        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], w[b][k1]);
         dft<C, -1>(v[b]);
 #pragma unroll
         for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);

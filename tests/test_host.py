@@ -83,9 +83,11 @@ def test_field_helpers_convention():
 
 
 def _header_symbols():
-    src = open(os.path.join(ROOT, "include", "gnlse.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(gnlse_\w+)\s*\(", src,
-                                 re.M)))
+    syms = set()
+    for h in ("gnlse.h", "sno.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        syms |= set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+((?:gnlse|sno)_\w+)\s*\(", src, re.M))
+    return sorted(syms)
 
 
 def test_abi_library_exports_every_declared_symbol():
