@@ -360,6 +360,14 @@ def run_ours(a):
         acc = {"members": len(idx), "median": statistics.median(errs), "max": max(errs),
                "frac_le_1e-4": sum(e <= 1e-4 for e in errs) / len(errs),
                "per_member": [float("%.3e" % e) for e in errs]}
+        # conditioning of the same members: the FP64 oracle's output change when only
+        # the input is rounded to complex64 (tests/golden/make_ensemble_conditioning.py)
+        try:
+            with open(os.path.join(ROOT, "tests", "golden", "ensemble_conditioning.json")) as f:
+                cond = {r["member"]: r["output_spectral_rel_change"] for r in json.load(f)["results"]}
+            acc["c64_input_sensitivity"] = [float("%.3e" % cond[i]) if i in cond else None for i in idx]
+        except OSError:
+            pass
 
     # plain single-instance GPU path (one library call per reference operation),
     # bounded per-attempt samples per grid size x this run's per-member attempt counts

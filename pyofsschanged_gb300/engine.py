@@ -190,12 +190,14 @@ class Plan:
                   "gnlse_get_stats")
         return [arr[i].as_dict() for i in range(len(self.instances))]
 
-    def instance_traces(self, i, stats=None):
-        """(z values, fields) of instance i's stored traces, as numpy arrays."""
+    def instance_traces(self, i, stats=None, device=False):
+        """(z values, fields) of instance i's stored traces, as numpy arrays
+        (fields as a [k, n] device tensor view with ``device=True``)."""
         st = (stats or self.stats())[i]
         k = st["ntraces"]
         if self.traces is None or k == 0:
-            return np.zeros(0), np.zeros((0, self.n[i]), complex)
+            empty = np.zeros((0, self.n[i]), complex)
+            return np.zeros(0), (torch.as_tensor(empty, device=self.device) if device else empty)
         z = self.trace_z[self.tracez_off[i]:self.tracez_off[i] + k].cpu().numpy()
-        f = self.traces[self.trace_off[i]:self.trace_off[i] + k * self.n[i]]
-        return z, f.view(k, self.n[i]).cpu().numpy()
+        f = self.traces[self.trace_off[i]:self.trace_off[i] + k * self.n[i]].view(k, self.n[i])
+        return z, (f if device else f.cpu().numpy())

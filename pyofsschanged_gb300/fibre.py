@@ -19,6 +19,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from .characteristics import trace_characteristics
 from .engine import Instance, Plan
 from .operators import GridTables
 
@@ -55,8 +56,13 @@ def raise_for_status(status):
         raise nat.GnlseError(status, "propagation")
 
 
+CHARACT_LISTS = ("energy_list", "max_power_list", "peaks_list", "duration_list", "spec_width_list",
+                 "l_nl_list", "l_d_list")
+
+
 class Storage:
-    """Trace store with the fields pyofss's Storage exposes (storage.py:140-192)."""
+    """Trace store with the fields pyofss's Storage exposes (storage.py:140-165), including
+    the per-trace characteristics of ``update_characts`` (storage.py:195-209)."""
 
     def __init__(self):
         self.z = []
@@ -64,12 +70,27 @@ class Storage:
         self.step_sizes = []
         self.fft_total = 0
         self.domain = None
+        for k in CHARACT_LISTS:
+            setattr(self, k, [])
 
     def __call__(self, domain):
         self.domain = domain
 
     def reset_array(self):
         self.z, self.As = [], []
+
+    def reset_characts(self):
+        for k in CHARACT_LISTS:
+            setattr(self, k, [])
+
+    def get_df(self, type="complex", z_curr=0):
+        """storage.py:250-268 for type 'complex' (needs pandas, like the reference)."""
+        import pandas as pd
+        if type != "complex":
+            raise NotImplementedError("only the complex-field dataframe is produced")
+        arr_z = np.array(self.z) * 10 ** 6 + z_curr  # mm
+        index = pd.MultiIndex.from_product([arr_z], names=["z [mm]"])
+        return pd.DataFrame(self.As, index=index)
 
 
 class _StepperView:
@@ -150,9 +171,15 @@ class Fibre:
         self.stepper.stats = st
         storage = self.stepper.storage
         storage.reset_array()
-        z, As = plan.instance_traces(0, stats)
+        storage.reset_characts()
+        z, As = plan.instance_traces(0, stats, device=True)
         storage.z = list(z)
-        storage.As = [a.astype(complex) for a in As]
+        storage.As = [a.astype(complex) for a in As.cpu().numpy()]
+        if len(z):
+            beta2 = self.beta[2] if self.beta is not None and len(self.beta) > 2 else None
+            ch = trace_characteristics(As, domain, self.gamma, beta2)
+            for k in CHARACT_LISTS:
+                setattr(storage, k, ch[k])
         if self.stepper.adaptive:
             storage.step_sizes = []
         storage.fft_total = int(st["evals"]) * 16

@@ -15,7 +15,7 @@ import torch
 
 import golden_cases as gc
 from oracle import gnlse_oracle as go
-from pyofsschanged_gb300 import Domain, GridTables, Instance, Plan
+from pyofsschanged_gb300 import Domain, GridTables, Instance, Plan, Sech
 
 pytestmark = pytest.mark.gpu
 
@@ -197,3 +197,29 @@ def test_nonfinite_input_reports_small_step(cuda_ready):
     st = plan.stats()[0]
     assert st["status"] == 1  # SmallStepSizeError
     assert st["finished"] == 1
+
+
+@pytest.mark.parametrize("n,precision,cluster,tol", [
+    (16384, "mixed", 8, FP32_SPEC_TOL),   # the 2^14 ensemble class: 8 CTAs x 2048 points
+    (16384, "mixed", 4, FP32_SPEC_TOL),
+    (8192, "mixed", 4, FP32_SPEC_TOL),    # the 2^13 ensemble class: 4 CTAs x 2048 points
+    (32768, "fp64", 8, FP64_TOL),         # 8 CTAs x 4096 points, complex128
+    (16384, "fp32", 4, FP32_SPEC_TOL)])
+def test_large_cluster_classes_match_oracle(cuda_ready, n, precision, cluster, tol):
+    """Raman + self-steepening fixed-step RK4IP on the ensemble's grid spacing, 20 steps."""
+    from pyofsschanged_gb300.ensemble import DT, FIBRE_835
+    d = Domain(bit_width=DT * n, samples_per_bit=n, centre_nu=go.lambda_to_nu(835.0))
+    a0 = Sech(peak_power=8.0e3, width=0.04, using_fwhm=True)(d, np.zeros(n, complex))
+    length, steps = 4.0e-6, 20
+    grid = go.Grid(bit_width=DT * n, samples_per_bit=n, centre_nu=go.lambda_to_nu(835.0))
+    want, _ = go.Propagator(grid, length, **FIBRE_835).standard(a0.copy(), steps)
+    plan = Plan([GridTables(d, cluster=cluster, **FIBRE_835)],
+                [Instance(0, method="rk4ip", length=length, total_steps=steps)], precision=precision)
+    assert plan.class_times()[0][1] == cluster
+    f = plan.pack([a0])
+    plan.propagate(f)
+    st = plan.stats()[0]
+    got = plan.unpack(f)[0].cpu().numpy().astype(complex)
+    assert st["status"] == 0 and st["evals"] == steps
+    err = rel_l2(got, want) if precision == "fp64" else spec_err(got, want)
+    assert err <= tol, err
