@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-attempts", type=int, default=20,
                     help="attempts per grid size timed on the plain single-instance GPU path")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="use the library's built-in class costs instead of measuring them first")
     ap.add_argument("--no-graph", dest="graph", action="store_false",
                     help="launch the timed steps eagerly instead of replaying a CUDA graph")
     ap.add_argument("--cluster", default="",
@@ -224,6 +226,16 @@ def run_ours(a):
     members, domains, fields = sc_ensemble(a.members)
     cluster = {int(k): int(v) for k, v in (kv.split(":") for kv in a.cluster.split(",") if kv)}
     grids, inst = ensemble_plan_inputs(members, domains, cluster=cluster)
+    tuned = None
+    if a.autotune and not cluster:
+        # measured SM time per attempt of every compiled class of each grid (untimed)
+        from pyofsschanged_gb300.autotune import autotune
+        samples = {}
+        for g in grids:
+            idx = [i for i, m in enumerate(members) if m.n == g.n][:8]
+            samples[g.n] = (g, [fields[i] for i in idx])
+        tuned = {f"{n}:{c}": round(us, 1) for (n, c), us in
+                 autotune(samples, a.precision, device=local).items()}
     plan = Plan(grids, inst, precision=a.precision, device=local)
     src = plan.pack(fields)
     work = torch.empty_like(src)
@@ -415,6 +427,7 @@ def run_ours(a):
                        "grids": "2^12/2^13/2^14 mixed, dt=12.5ps/8192, 835 nm",
                        "l2": "256 MiB buffer written between steps",
                        "launch": "CUDA graph replay per step" if graph is not None else "eager",
+                       "class_sm_us_per_attempt": tuned,
                        "evals_per_step": evals},
             "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
             "gpu_launches": launches, "accuracy_vs_fp64": acc, "plain": plain,

@@ -170,6 +170,16 @@ int gnlse_set_timing(gnlse_plan* plan, int enable);
 int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t* cluster,
                       int32_t* count, double* ms);
 
+/* Launch-class autotuning.  No counterpart in the reference (pyofss has no
+ * launch configuration).  A class is a compiled (precision, points per CTA,
+ * cluster size) instantiation; gnlse_class_supported tells whether one exists.
+ * gnlse_set_class_cost records a measured SM time (us) per attempt of one field
+ * in that class (sm_us <= 0 clears it); plans created afterwards choose each
+ * instance's class from these measurements instead of the built-in GB300 table
+ * (process-wide, thread-safe).  pyofsschanged_gb300.autotune measures them. */
+int gnlse_class_supported(int precision, int log2_points_per_cta, int cluster);
+int gnlse_set_class_cost(int precision, int log2_points_per_cta, int cluster, double sm_us);
+
 /* Phase cycle counters of builds compiled with GNLSE_PROF=1 (8 per instance:
  * transforms, stage loops, exp(hD) tables, whole kernel); GNLSE_UNSUPPORTED
  * in normal builds.  Synchronises the device. */

@@ -92,6 +92,8 @@ SIGNATURES = {
     "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
+    "gnlse_class_supported": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int]),
+    "gnlse_set_class_cost": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double]),
     # spectral neural operator surrogate kernels (include/sno.h)
     "sno_gemm": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
                             ct.c_void_p, ct.c_longlong, ct.c_longlong,

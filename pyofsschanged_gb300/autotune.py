@@ -1,0 +1,102 @@
+"""Launch-class autotuner: measured SM time per attempt for each candidate class.
+
+A grid of n points can run in several compiled classes (points per CTA x
+cluster size, e.g. 2^14 as 4 x 4096 or 8 x 2048).  For every grid and every
+compiled class this fills the GPU with copies of the caller's sample fields,
+times a fixed number of ARK4IP attempts per member with CUDA events and
+records ``SMs x time / attempts`` -- the SM time one attempt costs when the
+GPU is saturated -- in the library (``gnlse_set_class_cost``), so the plans
+created afterwards pick each instance's class from measurements on this GPU
+rather than from the built-in table.  Results can be cached in a JSON file.
+"""
+
+import copy
+import json
+import math
+import os
+
+import torch
+
+from . import _native as nat
+from .engine import PRECISIONS, Instance, Plan
+
+
+def candidates(n, precision):
+    """(log2 points per CTA, cluster size) classes compiled for an n-point grid."""
+    lib = nat.lib()
+    p = PRECISIONS[precision]
+    out = []
+    for c in (1, 2, 4, 8):
+        m = n // c
+        if m < 256 or m * c != n:
+            continue
+        logm = int(round(math.log2(m)))
+        if lib.gnlse_class_supported(p, logm, c):
+            out.append((logm, c))
+    return out
+
+
+def measure(grid, fields, cluster, precision, attempts=8, ctas_per_sm=4, device=None):
+    """SM time (us) per attempt of the grid in the given cluster size, GPU saturated."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    g = copy.copy(grid)
+    g.cluster = cluster
+    reps = max(1, math.ceil(ctas_per_sm * nsm / (cluster * len(fields))))
+    flist = list(fields) * reps
+    inst = [Instance(0, method="ark4ip", length=1.0, local_error=1e-6, weight=1.0) for _ in flist]
+    plan = Plan([g], inst, precision=precision, device=dev.index)
+    f = plan.pack(flist)
+    plan.reset()
+    plan.propagate(f, max_attempts=2, reset=False)
+    torch.cuda.synchronize(dev)
+    a0 = sum(s["attempts"] for s in plan.stats())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    plan.propagate(f, max_attempts=attempts, reset=False)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    done = sum(s["attempts"] for s in plan.stats()) - a0
+    return nsm * e0.elapsed_time(e1) * 1e3 / max(done, 1)
+
+
+def autotune(samples, precision="mixed", attempts=8, cache=None, device=None):
+    """samples: {n: (GridTables, [fields])}.  Measures every compiled class of every
+    grid, records the costs in the library and returns {(n, cluster): sm_us}.
+
+    With ``cache`` (a JSON path) results for this device and precision are reused
+    and new ones stored."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    key = f"{torch.cuda.get_device_name(dev)}|{precision}"
+    store = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as fh:
+            store = json.load(fh)
+    known = store.get(key, {})
+    res = {}
+    lib = nat.lib()
+    for n, (grid, fields) in sorted(samples.items()):
+        for logm, c in candidates(n, precision):
+            k = f"{n}:{c}"
+            us = known.get(k)
+            if us is None:
+                us = measure(grid, fields, c, precision, attempts, device=dev)
+                known[k] = us
+            res[(n, c)] = us
+            nat.check(lib.gnlse_set_class_cost(PRECISIONS[precision], logm, c, float(us)),
+                      "gnlse_set_class_cost")
+    if cache:
+        store[key] = known
+        with open(cache, "w") as fh:
+            json.dump(store, fh, indent=1)
+    return res
+
+
+def clear(precision="mixed"):
+    """Forget every recorded cost of a precision (plans fall back to the built-in table)."""
+    lib = nat.lib()
+    p = PRECISIONS[precision]
+    for logm in range(8, 14):
+        for c in (1, 2, 4, 8):
+            if lib.gnlse_class_supported(p, logm, c):
+                lib.gnlse_set_class_cost(p, logm, c, 0.0)

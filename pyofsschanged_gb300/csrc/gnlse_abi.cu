@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -31,7 +32,25 @@ struct ClassRun {
 // GB300 in mixed precision with the GPU saturated by fields of that class;
 // only ratios between classes are used.  Other classes: n log n scaling of the
 // 4096-point single-CTA figure, plus half again for a cluster exchange.
-double sm_cost(int logm, int C) {
+// Measured costs set by the caller's autotuner (gnlse_set_class_cost) take
+// precedence over the built-in table; process-wide, guarded by a mutex.
+struct CostEntry { int precision, logm, C; double us; };
+std::mutex g_cost_mu;
+std::vector<CostEntry> g_cost;
+
+bool tuned(int precision) {
+  std::lock_guard<std::mutex> lk(g_cost_mu);
+  for (const CostEntry& e : g_cost)
+    if (e.precision == precision) return true;
+  return false;
+}
+
+double sm_cost(int precision, int logm, int C) {
+  {
+    std::lock_guard<std::mutex> lk(g_cost_mu);
+    for (const CostEntry& e : g_cost)
+      if (e.precision == precision && e.logm == logm && e.C == C) return e.us;
+  }
   struct Entry { int logm, C; double us; };
   static const Entry tab[] = {{12, 1, 190.5}, {11, 2, 259.6},  {13, 1, 495.2},  {12, 2, 588.9},
                               {11, 4, 565.4}, {13, 2, 1496.0}, {12, 4, 1383.1}, {11, 8, 1331.4}};
@@ -290,6 +309,26 @@ const char* gnlse_status_string(int s) {
   }
 }
 
+int gnlse_class_supported(int precision, int log2_points_per_cta, int cluster) {
+  return supported(precision, log2_points_per_cta, cluster) ? 1 : 0;
+}
+
+int gnlse_set_class_cost(int precision, int log2_points_per_cta, int cluster, double sm_us) {
+  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED) return GNLSE_BAD_ARGUMENT;
+  if (!supported(precision, log2_points_per_cta, cluster)) return GNLSE_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_cost_mu);
+  for (size_t k = 0; k < g_cost.size(); ++k) {
+    CostEntry& e = g_cost[k];
+    if (e.precision == precision && e.logm == log2_points_per_cta && e.C == cluster) {
+      if (sm_us > 0) e.us = sm_us;
+      else g_cost.erase(g_cost.begin() + (long)k);
+      return GNLSE_OK;
+    }
+  }
+  if (sm_us > 0) g_cost.push_back({precision, log2_points_per_cta, cluster, sm_us});
+  return GNLSE_OK;
+}
+
 int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, int n_instances,
                       const gnlse_instance_desc* instances, gnlse_plan** plan_out) {
   if (!plan_out || !grids || !instances || n_grids <= 0 || n_instances <= 0) return GNLSE_BAD_ARGUMENT;
@@ -322,7 +361,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       tput[i] = lat[i] = C;
       continue;
     }
-    if (precision == GNLSE_FP64) {
+    if (precision == GNLSE_FP64 && !tuned(precision)) {
       // complex128: 4096 points per CTA (one CTA per SM), larger grids span a cluster
       const int C = n <= 4096 ? 1 : n / 4096;
       if (C > 8 || !supported(precision, ilog2i(n / C), C)) {
@@ -342,17 +381,17 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     for (int C = 1; C <= 8; C *= 2) {
       const int logm = ilog2i(n / C);
       if (n / C < 256 || logm > mcap || !supported(precision, logm, C)) continue;
-      if (!best || sm_cost(logm, C) < sm_cost(ilog2i(n / best), best)) best = C;
+      if (!best || sm_cost(precision, logm, C) < sm_cost(precision, ilog2i(n / best), best)) best = C;
     }
     if (!best) {
       free_plan(p);
       return GNLSE_UNSUPPORTED;
     }
-    const double cb = sm_cost(ilog2i(n / best), best);
+    const double cb = sm_cost(precision, ilog2i(n / best), best);
     for (int C = 1; C <= 8; C *= 2) {
       const int logm = ilog2i(n / C);
-      if (n / C < 256 || logm > mcap || !supported(precision, logm, C) || sm_cost(logm, C) > 1.5 * cb) continue;
-      if (!fast || sm_cost(logm, C) / C < sm_cost(ilog2i(n / fast), fast) / fast) fast = C;
+      if (n / C < 256 || logm > mcap || !supported(precision, logm, C) || sm_cost(precision, logm, C) > 1.5 * cb) continue;
+      if (!fast || sm_cost(precision, logm, C) / C < sm_cost(precision, ilog2i(n / fast), fast) / fast) fast = C;
     }
     tput[i] = best;
     lat[i] = fast;
@@ -417,7 +456,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   if (nsm <= 0) nsm = 1;
   std::vector<int> icl(n_instances);
   std::vector<double> w(n_instances);
-  auto icost = [&](int i, int C) { return sm_cost(ilog2i(grids[instances[i].grid].n / C), C); };
+  auto icost = [&](int i, int C) { return sm_cost(precision, ilog2i(grids[instances[i].grid].n / C), C); };
   auto chain = [&](int i, int C) { return 3.0 * w[i] * icost(i, C) / C; };
   double work = 0.0;
   for (int i = 0; i < n_instances; ++i) {
