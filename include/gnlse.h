@@ -170,6 +170,10 @@ int gnlse_set_timing(gnlse_plan* plan, int enable);
 int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t* cluster,
                       int32_t* count, double* ms);
 
+/* Name of the CUDA error behind the calling thread's last GNLSE_CUDA_ERROR or
+ * GNLSE_OUT_OF_MEMORY status ("none" before any). */
+const char* gnlse_last_cuda_error(void);
+
 /* Launch-class autotuning.  No counterpart in the reference (pyofss has no
  * launch configuration).  A class is a compiled (precision, points per CTA,
  * cluster size) instantiation; gnlse_class_supported tells whether one exists.

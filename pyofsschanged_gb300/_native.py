@@ -92,6 +92,7 @@ SIGNATURES = {
     "gnlse_class_times": (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
+    "gnlse_last_cuda_error": (ct.c_char_p, []),
     "gnlse_class_supported": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int]),
     "gnlse_set_class_cost": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double]),
     # spectral neural operator surrogate kernels (include/sno.h)
@@ -123,6 +124,8 @@ class GnlseError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
         msg = status_string(code) if _lib is not None else str(code)
+        if _lib is not None and code in (GNLSE_CUDA_ERROR, GNLSE_OUT_OF_MEMORY):
+            msg += " [" + _lib.gnlse_last_cuda_error().decode() + "]"
         super().__init__(f"{what}: {msg} (status {code})" if what else f"{msg} (status {code})")
 
 

@@ -22,13 +22,15 @@ from .engine import PRECISIONS, Instance, Plan
 
 
 def candidates(n, precision):
-    """(log2 points per CTA, cluster size) classes compiled for an n-point grid."""
+    """(log2 points per CTA, cluster size) classes compiled for an n-point grid that
+    plan creation may choose (at most 4096 points per CTA up to 8 x 4096-point grids)."""
     lib = nat.lib()
     p = PRECISIONS[precision]
+    mcap = 8192 if n > 8 * 4096 else 4096
     out = []
     for c in (1, 2, 4, 8):
         m = n // c
-        if m < 256 or m * c != n:
+        if m < 256 or m > mcap or m * c != n:
             continue
         logm = int(round(math.log2(m)))
         if lib.gnlse_class_supported(p, logm, c):
@@ -36,13 +38,16 @@ def candidates(n, precision):
     return out
 
 
-def measure(grid, fields, cluster, precision, attempts=8, ctas_per_sm=4, device=None):
-    """SM time (us) per attempt of the grid in the given cluster size, GPU saturated."""
+def measure(grid, fields, cluster, precision, attempts=8, ctas=32, device=None):
+    """SM time (us) per attempt of the grid in the given cluster size, GPU saturated.
+
+    The launch holds ``ctas`` CTAs per SM (several waves of resident CTAs of any
+    class), so the partial last wave costs little of the measured time."""
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
     g = copy.copy(grid)
     g.cluster = cluster
-    reps = max(1, math.ceil(ctas_per_sm * nsm / (cluster * len(fields))))
+    reps = max(1, math.ceil(ctas * nsm / (cluster * len(fields))))
     flist = list(fields) * reps
     inst = [Instance(0, method="ark4ip", length=1.0, local_error=1e-6, weight=1.0) for _ in flist]
     plan = Plan([g], inst, precision=precision, device=dev.index)

@@ -148,7 +148,21 @@ struct gnlse_plan {
 
 namespace {
 
+// Timing event record: under stream capture as an external event node (so the
+// graph's replays record it), otherwise a plain record.
+cudaError_t record_timing(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return e;
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
+// name of the CUDA error behind the last GNLSE_CUDA_ERROR / GNLSE_OUT_OF_MEMORY
+thread_local const char* g_last_cuda_error = "none";
+
 int cuda_fail(cudaError_t e) {
+  g_last_cuda_error = cudaGetErrorName(e);
   if (e == cudaErrorMemoryAllocation) return GNLSE_OUT_OF_MEMORY;
   return GNLSE_CUDA_ERROR;
 }
@@ -308,6 +322,8 @@ const char* gnlse_status_string(int s) {
     default: return "unknown status";
   }
 }
+
+const char* gnlse_last_cuda_error(void) { return g_last_cuda_error; }
 
 int gnlse_class_supported(int precision, int log2_points_per_cta, int cluster) {
   return supported(precision, log2_points_per_cta, cluster) ? 1 : 0;
@@ -643,17 +659,17 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
   kp.max_attempts = max_attempts;
   kp.prof = p->d_prof;
   cudaError_t e;
-  // Timing events are recorded as external events, so that under stream capture
-  // they become event-record nodes of the graph and still time each replay
+  // Under stream capture the timing events are recorded as external events, so
+  // that they become event-record nodes of the graph and still time each replay
   // (a plain record during capture only expresses a dependency).
   if (p->classes.size() == 1) {
     const ClassRun& c = p->classes[0];
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
-    if (p->timing && (e = cudaEventRecordWithFlags(p->t0[0], s, cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = record_timing(p->t0[0], s)) != cudaSuccess) return cuda_fail(e);
     e = dispatch(p->precision, c.logm, c.C, kp, c.count, s);
     if (e != cudaSuccess) return cuda_fail(e);
-    if (p->timing && (e = cudaEventRecordWithFlags(p->t1[0], s, cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = record_timing(p->t1[0], s)) != cudaSuccess) return cuda_fail(e);
     return GNLSE_OK;
   }
   // several classes: fork onto side streams so they share the GPU, then join
@@ -663,9 +679,9 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     if ((e = cudaStreamWaitEvent(p->side[k], p->fork, 0)) != cudaSuccess) return cuda_fail(e);
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
-    if (p->timing && (e = cudaEventRecordWithFlags(p->t0[k], p->side[k], cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = record_timing(p->t0[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k])) != cudaSuccess) return cuda_fail(e);
-    if (p->timing && (e = cudaEventRecordWithFlags(p->t1[k], p->side[k], cudaEventRecordExternal)) != cudaSuccess) return cuda_fail(e);
+    if (p->timing && (e = record_timing(p->t1[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaEventRecord(p->ev[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaStreamWaitEvent(s, p->ev[k], 0)) != cudaSuccess) return cuda_fail(e);
   }

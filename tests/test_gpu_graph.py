@@ -30,8 +30,10 @@ def test_graph_replay_matches_eager(cuda_ready):
     plan, src = _plan()
     budget = 25
     eager = src.clone()
+    plan.set_timing(True)  # per-class timing events, eager and (below) captured
     plan.propagate(eager, max_attempts=budget)
     torch.cuda.synchronize()
+    assert all(ms > 0 for (_, _, _, ms) in plan.class_times())
     ref = eager.cpu().numpy()
     ref_stats = [(s["attempts"], s["z"], s["h"]) for s in plan.stats()]
     assert len(plan.class_times()) >= 2  # several class launches: the fork/join path
@@ -44,8 +46,7 @@ def test_graph_replay_matches_eager(cuda_ready):
         plan.propagate(work, max_attempts=budget)
     torch.cuda.current_stream().wait_stream(side)
     torch.cuda.synchronize()
-    plan.set_timing(True)  # per-class timing events become nodes of the graph
-    g = torch.cuda.CUDAGraph()
+    g = torch.cuda.CUDAGraph()  # the timing events become event-record nodes of the graph
     with torch.cuda.graph(g):
         work.copy_(src)
         plan.propagate(work, max_attempts=budget)
