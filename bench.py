@@ -31,6 +31,9 @@ METRIC = "GNLSE ensemble solves/s on 1 GB300 (fused vs plain, <=1e-4 rel spectra
 UNIT = "solves/s"
 WORKLOAD = "sc_ensemble_256_ragged_2^12-2^14_ark4ip_1e-6"
 L2_FLUSH_BYTES = 256 << 20
+# dram__bytes_read.sum + dram__bytes_write.sum per ARK4IP attempt of one member, from
+# one ncu capture per class (profiles/); used to scale the dominant launch's traffic
+DRAM_BYTES_PER_ATTEMPT = {("mixed", 11, 8): 1.3117e9 / 530}
 
 
 def parse():
@@ -302,20 +305,20 @@ def run_ours(a):
     ms_step = ms_total / a.steps
     value = world * a.members * a.steps / (ms_total * 1e-3)
 
-    # roofline of the dominant kernel (largest share of kernel time)
-    n_by_cls = {}
-    for i, s in enumerate(stats):
-        g = plan.grids[plan.instances[i].grid]
-        n_by_cls.setdefault(g.n, 0)
-        n_by_cls[g.n] += s["evals"] * 2 * g.n * (8 if a.precision == "fp32" else 16)
-    per_cls = {}
-    for step_times in class_ms:
-        for (logm, c, cnt, ms) in step_times:
-            per_cls.setdefault((logm, c, cnt), []).append(ms)
-    dom = max(per_cls, key=lambda k: sum(per_cls[k]))
-    dom_ms = statistics.mean(per_cls[dom])
-    dom_n = (1 << dom[0]) * dom[1]
-    alg_bytes = n_by_cls[dom_n]
+    # roofline of the dominant launch: the class launch with the most algorithmic
+    # bytes (RK4IP evaluations x 2 x N x element size), timed by its own CUDA events
+    vsz = 8 if a.precision == "fp32" else 16
+    members_of = plan.class_members()
+    launches_t = class_ms[-1]
+    best = None
+    for k, (logm, c, cnt, _) in enumerate(launches_t):
+        ids = members_of[k]
+        n = (1 << logm) * c
+        b = sum(stats[i]["evals"] * 2 * n * vsz for i in ids)
+        if best is None or b > best[0]:
+            best = (b, k, logm, c, n, ids)
+    alg_bytes, dom_k, dom_logm, dom_c, dom_n, dom_ids = best
+    dom_ms = statistics.mean(st[dom_k][3] for st in class_ms)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -324,15 +327,15 @@ def run_ours(a):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
-    fft_flops = 0.0
-    for i, s in enumerate(stats):
-        n = plan.grids[plan.instances[i].grid].n
-        if n == dom_n:
-            fft_flops += s["evals"] * 16 * 5.0 * n * math.log2(n)
+    fft_flops = sum(stats[i]["evals"] * 16 * 5.0 * dom_n * math.log2(dom_n) for i in dom_ids)
+    # DRAM bytes per attempt from one ncu capture of this class (a 10-attempt launch of
+    # 53 members; profiles/gnlse_kernel_mixed_m11_c8_ensemble.md), scaled to this launch
+    per_attempt = DRAM_BYTES_PER_ATTEMPT.get((a.precision, dom_logm, dom_c))
+    traffic = per_attempt * sum(stats[i]["attempts"] for i in dom_ids) if per_attempt else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
-                "kernel": f"gnlse_kernel<{'double' if a.precision == 'fp64' else 'float'},{dom[0]},{dom[1]},{'true' if a.precision == 'mixed' else 'false'}>",
-                "launch_ms": dom_ms, "alg_bytes_per_launch": alg_bytes,
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel": f"gnlse_kernel<{'double' if a.precision == 'fp64' else 'float'},{dom_logm},{dom_c},{'true' if a.precision == 'mixed' else 'false'}>",
+                "launch_ms": dom_ms, "alg_bytes_per_launch": alg_bytes, "members": len(dom_ids),
                 "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback",
                 "fft_gflops": fft_flops / (dom_ms * 1e-3) / 1e9}
 

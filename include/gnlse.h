@@ -170,6 +170,10 @@ int gnlse_set_timing(gnlse_plan* plan, int enable);
 int gnlse_class_times(gnlse_plan* plan, int max_classes, int32_t* logm, int32_t* cluster,
                       int32_t* count, double* ms);
 
+/* Instance indices in launch order (n_instances entries): launch k of
+ * gnlse_class_times covers the next count[k] entries. */
+int gnlse_class_order(gnlse_plan* plan, int32_t* order);
+
 /* Name of the CUDA error behind the calling thread's last GNLSE_CUDA_ERROR or
  * GNLSE_OUT_OF_MEMORY status ("none" before any). */
 const char* gnlse_last_cuda_error(void);

@@ -93,6 +93,7 @@ SIGNATURES = {
                                      ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32),
                                      ct.POINTER(ct.c_double)]),
     "gnlse_last_cuda_error": (ct.c_char_p, []),
+    "gnlse_class_order": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int32)]),
     "gnlse_class_supported": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int]),
     "gnlse_set_class_cost": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double]),
     # spectral neural operator surrogate kernels (include/sno.h)

@@ -747,6 +747,12 @@ int gnlse_class_times(gnlse_plan* p, int max_classes, int32_t* logm, int32_t* cl
   return nc;
 }
 
+int gnlse_class_order(gnlse_plan* p, int32_t* order) {
+  if (!p || !order) return GNLSE_BAD_ARGUMENT;
+  for (size_t i = 0; i < p->order.size(); ++i) order[i] = p->order[i];
+  return GNLSE_OK;
+}
+
 int gnlse_get_stats(gnlse_plan* p, gnlse_stats* out, void* stream) {
   if (!p || !out) return GNLSE_BAD_ARGUMENT;
   const size_t n = p->inst.size();

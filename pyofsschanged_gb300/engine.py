@@ -183,6 +183,17 @@ class Plan:
             raise nat.GnlseError(-nc, "gnlse_class_times")
         return [(lm[i], cl[i], cnt[i], ms[i]) for i in range(nc)]
 
+    def class_members(self):
+        """Instance indices of each launch, in the order of class_times()."""
+        n = len(self.instances)
+        order = (ct.c_int32 * n)()
+        nat.check(nat.lib().gnlse_class_order(self.handle, order), "gnlse_class_order")
+        out, k = [], 0
+        for (_, _, cnt, _) in self.class_times():
+            out.append(list(order[k:k + cnt]))
+            k += cnt
+        return out
+
     def stats(self, stream=None):
         s = stream or torch.cuda.current_stream(self.device)
         arr = (nat.Stats * len(self.instances))()
