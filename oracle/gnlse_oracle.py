@@ -358,14 +358,32 @@ class Propagator:
         k3 = h * self.n(self.linear(A_I + k2, hh))
         return (k3 / 6.0) + self.linear(A_I + (k0 + 2.0 * (k1 + k2)) / 6.0, hh)
 
+    @staticmethod
+    def rk4(A, h, f):
+        """``Solver.rk4`` (solver.py:109-116) for an autonomous f."""
+        k0 = h * f(A)
+        k1 = h * f(A + 0.5 * k0)
+        k2 = h * f(A + 0.5 * k1)
+        k3 = h * f(A + k2)
+        return A + (k0 + 2.0 * (k1 + k2) + k3) / 6.0
+
+    def ss_sym_rk4(self, A, h):
+        """``Solver.ss_sym_rk4`` (solver.py:330-337): linear half step, classical RK4 on
+        the nonlinear term, linear half step."""
+        self.evals += 1
+        A_L = self.linear(A, 0.5 * h)
+        A_N = self.rk4(A_L, h, self.n)
+        return self.linear(A_N, 0.5 * h)
+
     # -- fixed step (stepper.py:164-221) --------------------------------------
-    def standard(self, A, total_steps, traces=1):
+    def standard(self, A, total_steps, traces=1, method="rk4ip"):
         h = self.length / total_steps
         zs = np.linspace(0.0, self.length, total_steps + 1)
         storage_step = int(total_steps / traces)
         trace_z, trace_A = [], []
+        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4}[method]
         for i, z in enumerate(zs[:-1]):
-            A = self.rk4ip(A, h)
+            A = step(A, h)
             if traces != 1 and i % storage_step == 0:
                 trace_z.append(z + h)
                 trace_A.append(A)

@@ -421,11 +421,16 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   int64_t foff = 0, soff = 0, toff = 0, zoff = 0;
   for (int i = 0; i < n_instances; ++i) {
     const gnlse_instance_desc& id = instances[i];
-    if (id.grid < 0 || id.grid >= n_grids || (id.method != GNLSE_RK4IP && id.method != GNLSE_ARK4IP) ||
+    if (id.grid < 0 || id.grid >= n_grids ||
+        (id.method != GNLSE_RK4IP && id.method != GNLSE_ARK4IP && id.method != GNLSE_SS_SYM_RK4) ||
         id.total_steps < 1 || id.traces < 1 || id.max_traces < 0 || !(id.length >= 0) ||
         (id.method == GNLSE_ARK4IP && !(id.local_error > 0))) {
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
+    }
+    if (id.method == GNLSE_SS_SYM_RK4 && grids[id.grid].gain_on) {
+      free_plan(p);  // the split-step path has no amplifier step
+      return GNLSE_UNSUPPORTED;
     }
     const int n = grids[id.grid].n;
     InstDev& d = p->inst[i];

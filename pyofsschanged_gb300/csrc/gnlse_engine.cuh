@@ -912,6 +912,21 @@ struct Engine {
     __syncthreads();
   }
 
+  // dst = E dst over this CTA's slice: the linear half steps of the split-step method
+  static __device__ __noinline__ void scale_state(const Ctx& cx, SV* dst, const SV* E) {
+    const int base = cx.rank * M;
+    struct In { SL e, s; };
+    each_slot<4, In>([&](int l) { return In{lds(E, base + l), lds(dst, base + l)}; },
+                     [&](int l, const In& r) {
+                       if constexpr (XS) {
+                         dfc_store(dst, base + l, dfc_mul(r.e, r.s));
+                       } else {
+                         dst[base + l] = cmul(r.e, r.s);
+                       }
+                     });
+    __syncthreads();
+  }
+
   static __device__ __forceinline__ void scale_stage3(const Ctx& cx, const Op& op) {
     const int base = cx.rank * M;
     for (int l = threadIdx.x; l < M; l += T) {
@@ -1115,7 +1130,14 @@ struct Engine {
     }
 
     const bool adaptive = d.method == 1;
-    if (st.phase == 1 && !adaptive) exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
+    // Solver.ss_sym_rk4 (solver.py:330-337): S <- E S, classical RK4 on the nonlinear
+    // term (the RK4IP stage algebra with the exp(hD/2) factors replaced by an exact 1,
+    // table 6), result <- E result, E = exp(hD/2) (table 7)
+    const bool ssrk = d.method == 2;
+    if (st.phase == 1 && !adaptive) {
+      exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
+      if (ssrk) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
+    }
 
     while (st.phase == 1 && budget > 0) {
       // ---- one attempt (adaptive) or one step (fixed) ------------------------
@@ -1142,6 +1164,7 @@ struct Engine {
       PROF_ADD(2);
       const int q_end = adaptive ? 11 : 4;
       double nrm[3] = {0.0, 0.0, 0.0};
+      if (ssrk) scale_state(cx, base + (long long)sidx * N, base + 7 * N);  // linear half step
       for (int q = st.ma_valid ? 1 : 0; q < q_end; ++q) {
         // slot q: kind 0 = N(A) of state mi, kind 1..3 = stage of evaluation e
         const int kind = (q == 0 || q == 4) ? 0 : (q < 4 ? q : (q < 8 ? q - 4 : q - 7));
@@ -1160,7 +1183,7 @@ struct Engine {
             op.Sf = base + 2 * N;
             op.S0 = e == 1 ? Sh : S;
             op.MA0 = reinterpret_cast<V*>(base + (3 + m) * N);
-            op.Et = base + ((adaptive && e < 2) ? 6 : 7) * N;
+            op.Et = base + ((ssrk || (adaptive && e < 2)) ? 6 : 7) * N;
             op.out = e == 1 ? base + 2 * N : Sh;
             op.h = (R)he;
             op.hh = 0.5 * he;
@@ -1215,6 +1238,7 @@ struct Engine {
         }
         PROF_ADD(1);
       }
+      if (ssrk) scale_state(cx, base + (long long)(sidx ^ 1) * N, base + 7 * N);  // linear half step
       budget -= 1;
 
       if (!adaptive) {

@@ -15,7 +15,7 @@ import torch
 from . import _native as nat
 
 PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE_MIXED}
-METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP}
+METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP, "ss_sym_rk4": nat.GNLSE_SS_SYM_RK4}
 
 
 def _ptr(a):
@@ -33,7 +33,7 @@ class Instance:
         self.weight = float(weight)
         self.method = method.lower()
         if self.method not in METHODS:
-            raise ValueError(f"unknown method {method!r} (rk4ip or ark4ip)")
+            raise ValueError(f"unknown method {method!r} (rk4ip, ark4ip or ss_sym_rk4)")
         self.length = float(length)
         self.local_error = float(local_error)
         self.total_steps = int(total_steps)
@@ -41,7 +41,7 @@ class Instance:
         if max_traces is None:
             if self.traces == 1:
                 max_traces = 0
-            elif self.method == "rk4ip":
+            elif self.method in ("rk4ip", "ss_sym_rk4"):  # fixed-step trace rule
                 step = self.total_steps // self.traces if self.traces else 0
                 max_traces = (self.total_steps + step - 1) // step if step > 0 else 0
             else:

@@ -39,3 +39,12 @@ def accepted_steps(calls, adaptive):
     zs, hs = att[:, 0, 0], att[:, 2, 1]
     acc = [i for i in range(len(zs) - 1) if zs[i + 1] > zs[i]] + [len(zs) - 1]
     return np.stack([zs[acc], hs[acc]], axis=1)
+
+
+def expected_evals(case):
+    """Solver evaluations of the reference run: its logged rk4ip calls, or one per fixed
+    step for the split-step method (which makes no rk4ip calls)."""
+    fk = case["params"]["fibre"]
+    if fk["method"] == "ss_sym_rk4":
+        return fk["total_steps"]
+    return len(case["rk4ip_calls"])

@@ -60,12 +60,14 @@ def test_fp64_matches_reference(cuda_ready, name):
     case = gc.load(name)
     plan, out, st = run(case, "fp64")
     assert st["status"] == 0 and st["finished"] == 1
-    assert st["evals"] == len(case["rk4ip_calls"])
+    assert st["evals"] == gc.expected_evals(case)
     assert rel_l2(out, case["A_out"]) <= FP64_TOL
     assert spec_err(out, case["A_out"]) <= FP64_TOL
 
 
 CHAOTIC = {"sc_hollenbeck_ark4ip_2048", "sc_cfg_8192"}
+# complex64 state through 2 x 800 linear half steps (plus the RK4 stages): 1.1e-4 measured
+FP32_SPLIT_STEP_TOL = 2e-4
 
 
 @pytest.mark.parametrize("name", FAST)
@@ -74,7 +76,7 @@ def test_mixed_matches_reference(cuda_ready, name):
     plan, out, st = run(case, "mixed")
     assert st["status"] == 0 and st["finished"] == 1
     assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
-    n_ref = len(case["rk4ip_calls"])
+    n_ref = gc.expected_evals(case)
     assert abs(st["evals"] - n_ref) <= max(3, 0.01 * n_ref)
 
 
@@ -83,9 +85,10 @@ def test_fp32_matches_reference(cuda_ready, name):
     case = gc.load(name)
     plan, out, st = run(case, "fp32")
     assert st["status"] == 0 and st["finished"] == 1
-    assert spec_err(out, case["A_out"]) <= (1e-3 if name in CHAOTIC else FP32_SPEC_TOL)
+    tol = 1e-3 if name in CHAOTIC else (FP32_SPLIT_STEP_TOL if name.startswith("ss_") else FP32_SPEC_TOL)
+    assert spec_err(out, case["A_out"]) <= tol
     # the step-size controller sees FP32 round-off; the attempt count stays close
-    n_ref = len(case["rk4ip_calls"])
+    n_ref = gc.expected_evals(case)
     assert abs(st["evals"] - n_ref) <= max(3, 0.05 * n_ref)
 
 
@@ -96,18 +99,20 @@ def test_fp32_matches_reference(cuda_ready, name):
     ("spm_loss_fixed_2048", "fp64", 2), ("sc_blowwood_fixed_4096", "fp64", 2),
     ("sc_blowwood_fixed_4096", "fp32", 1), ("soliton_test_solver_2048", "fp32", 1),
     ("sc_blowwood_ark4ip_1024", "mixed", 2), ("gain_ark4ip_1024", "mixed", 4),
-    ("sc_blowwood_fixed_4096", "mixed", 1)])
+    ("sc_blowwood_fixed_4096", "mixed", 1), ("ss_sym_rk4_sc_1024", "fp64", 2),
+    ("ss_sym_rk4_sc_1024", "mixed", 4), ("ss_sym_rk4_soliton_1024", "fp32", 2)])
 def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     case = gc.load(name)
     _, out, st = run(case, precision, cluster)
     assert st["status"] == 0
     if precision == "fp64":
-        assert st["evals"] == len(case["rk4ip_calls"])
+        assert st["evals"] == gc.expected_evals(case)
         assert rel_l2(out, case["A_out"]) <= FP64_TOL
     elif precision == "mixed":
         assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
     else:
-        assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
+        assert spec_err(out, case["A_out"]) <= (FP32_SPLIT_STEP_TOL if name.startswith("ss_")
+                                                 else FP32_SPEC_TOL)
 
 
 def test_fixed_step_traces(cuda_ready):
@@ -136,7 +141,7 @@ def test_sc_cfg_8192_all_precisions(cuda_ready):
     case = gc.load("sc_cfg_8192")
     _, out64, st64 = run(case, "fp64")
     assert st64["status"] == 0
-    assert st64["evals"] == len(case["rk4ip_calls"])
+    assert st64["evals"] == gc.expected_evals(case)
     assert rel_l2(out64, case["A_out"]) <= FP64_TOL
     # This propagation amplifies a 1e-7 relative perturbation of its input to a
     # 2.1e-4 change of the FP64 output (oracle, seeded complex Gaussian noise),
