@@ -434,7 +434,8 @@ def run_ours(a):
                        "evals_per_step": evals},
             "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
             "gpu_launches": launches, "accuracy_vs_fp64": acc, "plain": plain,
-            "class_ms": {f"m2^{k[0]}_c{k[1]}_n{k[2]}": statistics.mean(v) for k, v in per_cls.items()}}
+            "class_ms": {f"m2^{lm}_c{c}_n{cnt}": statistics.mean(st[k][3] for st in class_ms)
+                         for k, (lm, c, cnt, _) in enumerate(class_ms[0])}}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -227,6 +227,27 @@ struct Engine {
     }
   }
 
+  // Time-domain shared-memory layout: with C > 1 the CTA owning positions
+  // n2 in [rank*M/C, (rank+1)*M/C) holds every sample n1*M + n2 of them (n1 < C),
+  // at slot n1*M/C + n2 mod M/C, so both cross-CTA passes find their time-domain
+  // operands locally.  With C = 1 the slot is the sample index.
+  static __device__ __forceinline__ int tslot(int n1, int n2) {
+    if constexpr (C > 1) {
+      return n1 * (M / C) + (n2 & (M / C - 1));
+    } else {
+      return n2;
+    }
+  }
+  // global sample index of local time slot s of CTA rank
+  static __device__ __forceinline__ int tsample(int rank, int s) {
+    if constexpr (C > 1) {
+      constexpr int PM = M / C;
+      return (s / PM) * M + rank * PM + (s & (PM - 1));
+    } else {
+      return rank * M + s;
+    }
+  }
+
   static __device__ __forceinline__ void csync() {
     if constexpr (C > 1) {
       cg::this_cluster().sync();
@@ -365,46 +386,42 @@ struct Engine {
       csync();
       return;
     }
-    // all positions of a thread at once, so their remote loads overlap; the
-    // twiddles W_N^{n2 k1} are requested before the barrier
+    // Time-domain inputs are local (this CTA owns all C samples of its positions,
+    // see tslot), so the loads, the radix-C DFT and the twiddles run before the
+    // barrier that frees the other CTAs' exchange buffers; then the pushes.
     constexpr int BP = (PM + T - 1) / T;
     V v[BP][C];
-    V w[BP][C];
-#pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = tid + b * T;
-      if (PM % T == 0 || q < PM)
-#pragma unroll
-        for (int k1 = 1; k1 < C; ++k1) w[b][k1] = twid(cx.tw, (cx.rank * PM + q) * k1, +1);
-    }
-    if (lead) csync();
-#pragma unroll
-    for (int b = 0; b < BP; ++b) {
-      const int q = tid + b * T;
-      if (PM % T == 0 || q < PM)
-#pragma unroll
-        for (int r = 0; r < C; ++r) v[b][r] = pro(r, cx.rank * PM + q);
-    }
+    __syncthreads();  // inputs written by this CTA's threads
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
       const int q = tid + b * T;
       if (PM % T == 0 || q < PM) {
         const int n2 = cx.rank * PM + q;
+#pragma unroll
+        for (int r = 0; r < C; ++r) v[b][r] = pro(r, n2);
         dft<C, +1>(v[b]);
 #pragma unroll
-        for (int k1 = 0; k1 < C; ++k1) {
-          const V val = k1 ? cmul(v[b][k1], w[b][k1]) : v[b][k1];
-          rmt(cx.W, k1)[pad(n2)] = val;
-        }
+        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, +1));
+      }
+    }
+    csync();  // every CTA is done reading its exchange buffer
+#pragma unroll
+    for (int b = 0; b < BP; ++b) {
+      const int q = tid + b * T;
+      if (PM % T == 0 || q < PM) {
+        const int n2 = cx.rank * PM + q;
+#pragma unroll
+        for (int k1 = 0; k1 < C; ++k1) rmt(cx.W, k1)[pad(n2)] = v[b][k1];
       }
     }
     csync();
+    (void)lead;
   }
 
   // Inverse cross-CTA pass from the exchange buffers: exchange slot n2 of
   // every CTA k1 -> twiddle W_N^{-n2 k1} -> radix-C DFT -> epi(n1, n2, x[n1*M + n2]).
   template <class Epi>
-  static __device__ __forceinline__ void cross_inv(const Ctx& cx, Epi& epi) {
+  static __device__ __forceinline__ void cross_inv(const Ctx& cx, Epi& epi, bool trail = true) {
     constexpr int PM = M / C;
     const int tid = tidx<1>();
     if constexpr (INPLACE) {
@@ -464,13 +481,21 @@ struct Engine {
         for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
       }
     }
-    csync();
+    // The outputs are local (tslot); the cluster barrier is needed only when the
+    // next write into an exchange buffer is not a forward cross pass (which frees
+    // the buffers itself) -- trail = false skips it.
+    if (trail) {
+      csync();
+    } else {
+      __syncthreads();
+    }
   }
 
   // Forward transform G+(x)[k] = sum_n x[n] e^{+2 pi i k n / N} (= N * pyofss fft),
-  // result in buf (or to epi).  pro(owner, slot): time-domain input; epi(owner,
-  // slot, v): spectral output, always called in the owner CTA.  lead: inputs
-  // were written (locally) since the last cluster barrier.
+  // result in buf (or to epi).  pro(n1, n2): time sample n1*M + n2, asked for only
+  // in the CTA owning position n2 (tslot); epi(owner, slot, v): spectral output,
+  // always called in the owner CTA.  lead (in-place cross passes only): inputs were
+  // written since the last cluster barrier.
   template <class Pro, class Epi>
   static __device__ __forceinline__ void fwd(const Ctx& cx, V* buf, Pro& pro, Epi& epi, bool lead = true) {
     if constexpr (C == 1) {
@@ -482,15 +507,15 @@ struct Engine {
   }
 
   // Inverse transform G-(X)[n] = sum_k X[k] e^{-2 pi i k n / N} (= pyofss ifft).
-  // pro(owner, slot): spectral input (owner CTA); epi(owner, slot, v): time
-  // output, possibly for a remote CTA of the cluster.
+  // pro(owner, slot): spectral input (owner CTA); epi(n1, n2, v): time sample
+  // n1*M + n2, called in the CTA owning position n2 (tslot).
   template <class Pro, class Epi>
-  static __device__ __forceinline__ void inv(const Ctx& cx, V* buf, Pro& pro, Epi& epi) {
+  static __device__ __forceinline__ void inv(const Ctx& cx, V* buf, Pro& pro, Epi& epi, bool trail = true) {
     if constexpr (C == 1) {
       local_fft<-1, true, true>(cx, buf, buf, buf, pro, epi);
     } else {
       local_fft<-1, true, false>(cx, buf, buf, cx.W, pro, epi);
-      cross_inv(cx, epi);
+      cross_inv(cx, epi, trail);
     }
   }
 
@@ -591,30 +616,35 @@ struct Engine {
     const bool raman = g.raman != 0;
     V* X = cx.X;
     V* P = cx.P;
-    auto rdX = [&](int o, int l) -> V { return rmt(X, o)[pad(l)]; };
+    // spectral operands are read by the local passes of this CTA (slot l), time-domain
+    // ones by the cross-CTA passes as sample (n1, n2) at local slot tslot(n1, n2)
+    auto rdXs = [&](int, int l) -> V { return X[pad(l)]; };
+    auto rdXt = [&](int n1, int n2) -> V { return X[pad(tslot(n1, n2))]; };
     const bool keep_p = raman || want_e;
-    auto e1 = [&](int o, int l, V v) {
+    auto e1 = [&](int n1, int n2, V v) {
+      const int s = pad(tslot(n1, n2));
       V x = cscale(v, invN);
       R p = cabs2(x);
-      if (keep_p) rmt(P, o)[pad(l)] = mk<V>(p, (R)0);
-      rmt(X, o)[pad(l)] = raman ? x : cscale(x, p);
+      if (keep_p) P[s] = mk<V>(p, (R)0);
+      X[s] = raman ? x : cscale(x, p);
     };
-    inv(cx, X, rdX, e1);
+    inv(cx, X, rdXs, e1, false);  // the next exchange is a forward cross pass
     double energy = 0.0;
     if (want_e) energy = simpson_energy(cx, g, P);
     if (raman) {
       const V* Hp = (const V*)g.Hp;
       const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
-      auto rdP = [&](int o, int l) -> V { return rmt(P, o)[pad(l)]; };
-      auto wrP = [&](int o, int l, V v) { P[pad(l)] = v; };
-      fwd(cx, P, rdP, wrP, false);  // inv() ended with a cluster barrier
+      auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
+      auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
+      fwd(cx, P, rdPt, wrP, false);
 #if GNLSE_RAMAN_SPLIT
       // spectral product and time-domain combination as separate passes over
       // this CTA's slice (fewer live registers in the transform passes)
       for (int l = threadIdx.x; l < M; l += T) P[pad(l)] = cmul(P[pad(l)], __ldg(&Hp[cx.rank * M + l]));
       __syncthreads();
-      auto wrPt = [&](int o, int l, V v) { rmt(P, o)[pad(l)] = v; };
-      inv(cx, P, rdP, wrPt);
+      auto rdPs = [&](int, int l) -> V { return P[pad(l)]; };
+      auto wrPt = [&](int n1, int n2, V v) { P[pad(tslot(n1, n2))] = v; };
+      inv(cx, P, rdPs, wrPt, false);
       for (int l = threadIdx.x; l < M; l += T) {
         const V x = X[pad(l)], conv = P[pad(l)];
         const R p = cabs2(x);
@@ -623,25 +653,25 @@ struct Engine {
       __syncthreads();
 #else
       auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
-      auto e3 = [&](int o, int l, V conv) {
-        V* Xo = rmt(X, o);
-        V x = Xo[pad(l)];
+      auto e3 = [&](int n1, int n2, V conv) {
+        const int s = pad(tslot(n1, n2));
+        V x = X[s];
         R p = cabs2(x);
-        Xo[pad(l)] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
+        X[s] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
       };
-      inv(cx, P, rdPH, e3);
+      inv(cx, P, rdPH, e3, false);
 #endif
     }
-    auto wrX = [&](int o, int l, V v) { X[pad(l)] = v; };
-    fwd(cx, X, rdX, wrX, GNLSE_RAMAN_SPLIT && raman);  // inputs last written by inv() otherwise
+    auto wrX = [&](int, int l, V v) { X[pad(l)] = v; };
+    fwd(cx, X, rdXt, wrX, false);
     return energy;
   }
 
   // Simpson energy (nJ) of the time-domain powers held in buf[].x (this CTA's
-  // samples rank*M + l), summed over the cluster.
+  // local time slots, sample tsample(rank, slot)), summed over the cluster.
   static __device__ double simpson_energy(const Ctx& cx, const GridDev& g, const V* buf) {
     double e = 0.0;
-    for (int l = threadIdx.x; l < M; l += T) e += simpson_w(cx.rank * M + l, N) * (double)buf[pad(l)].x;
+    for (int l = threadIdx.x; l < M; l += T) e += simpson_w(tsample(cx.rank, l), N) * (double)buf[pad(l)].x;
     double s[1] = {e * g.dt * 1e-3};
     cluster_sum<1>(cx, s);
     return s[0];
@@ -655,7 +685,7 @@ struct Engine {
     auto pl = [&](int o, int l) -> V {
       return src == 0 ? op.MA0[o * M + l] : (src == 1 ? ldv(op.acc, o * M + l) : cx.X[pad(l)]);
     };
-    auto ep = [&](int o, int l, V v) { rmt(P, o)[pad(l)] = mk<V>(cabs2(cscale(v, invN)), (R)0); };
+    auto ep = [&](int n1, int n2, V v) { P[pad(tslot(n1, n2))] = mk<V>(cabs2(cscale(v, invN)), (R)0); };
     inv(cx, P, pl, ep);
     return simpson_energy(cx, g, P);
   }
