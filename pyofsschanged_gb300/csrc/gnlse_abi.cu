@@ -52,8 +52,8 @@ double sm_cost(int precision, int logm, int C) {
       if (e.precision == precision && e.logm == logm && e.C == C) return e.us;
   }
   struct Entry { int logm, C; double us; };
-  static const Entry tab[] = {{12, 1, 190.5}, {11, 2, 259.6},  {13, 1, 495.2},  {12, 2, 588.9},
-                              {11, 4, 565.4}, {13, 2, 1496.0}, {12, 4, 1383.1}, {11, 8, 1331.4}};
+  static const Entry tab[] = {{12, 1, 171.4}, {11, 2, 198.3},  {13, 1, 495.2},  {12, 2, 514.9},
+                              {11, 4, 457.9}, {13, 2, 1496.0}, {12, 4, 1158.3}, {11, 8, 992.6}};
   for (const Entry& e : tab)
     if (e.logm == logm && e.C == C) return e.us;
   const double n = (double)(1 << logm) * C;
