@@ -356,7 +356,7 @@ struct Engine {
   // -> exchange slot n2 of CTA k1.  lead: a cluster barrier is needed first
   // (inputs written since the last one).
   template <class Pro>
-  static __device__ __forceinline__ void cross_fwd(const Ctx& cx, Pro& pro, bool lead) {
+  static __device__ __forceinline__ void cross_fwd(const Ctx& cx, Pro& pro, bool lead, bool wfree = true) {
     constexpr int PM = M / C;
     const int tid = tidx<1>();
     if constexpr (INPLACE) {
@@ -404,7 +404,7 @@ struct Engine {
         for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, +1));
       }
     }
-    csync();  // every CTA is done reading its exchange buffer
+    if (wfree) csync();  // every CTA is done reading its exchange buffer
 #pragma unroll
     for (int b = 0; b < BP; ++b) {
       const int q = tid + b * T;
@@ -495,14 +495,53 @@ struct Engine {
   // result in buf (or to epi).  pro(n1, n2): time sample n1*M + n2, asked for only
   // in the CTA owning position n2 (tslot); epi(owner, slot, v): spectral output,
   // always called in the owner CTA.  lead (in-place cross passes only): inputs were
-  // written since the last cluster barrier.
+  // written since the last cluster barrier.  wfree = false: the caller guarantees that
+  // no CTA still reads its exchange buffer (its last readers finished before a cluster
+  // barrier already passed).
   template <class Pro, class Epi>
-  static __device__ __forceinline__ void fwd(const Ctx& cx, V* buf, Pro& pro, Epi& epi, bool lead = true) {
+  static __device__ __forceinline__ void fwd(const Ctx& cx, V* buf, Pro& pro, Epi& epi, bool lead = true,
+                                             bool wfree = true) {
     if constexpr (C == 1) {
       local_fft<+1, true, true>(cx, buf, buf, buf, pro, epi);
     } else {
-      cross_fwd(cx, pro, lead);
+      cross_fwd(cx, pro, lead, wfree);
       local_fft<+1, false, true>(cx, cx.W, buf, buf, pro, epi);
+    }
+  }
+
+  // Inverse transform whose exchange goes through the P buffers: local passes in place
+  // on buf, the last one pushing each output to the CTA owning its position (P slot
+  // tslot(rank, n2)), one cluster barrier, then the radix-C pass on this CTA's own P
+  // (each thread reads and rewrites only the C slots of its positions, so epi may write
+  // P).  Needs P free in every CTA until the barrier; the exchange buffers W are not
+  // touched.
+  template <class Pro, class Epi>
+  static __device__ __forceinline__ void inv_via_p(const Ctx& cx, V* buf, Pro& pro, Epi& epi) {
+    if constexpr (C == 1) {
+      local_fft<-1, true, true>(cx, buf, buf, buf, pro, epi);
+    } else {
+      constexpr int PM = M / C;
+      auto push = [&](int, int o, V v) { rmt(cx.P, o / PM)[pad(tslot(cx.rank, o))] = v; };
+      local_fft<-1, true, true>(cx, buf, buf, buf, pro, push);
+      csync();
+      const int tid = tidx<1>();
+      constexpr int BP = (PM + T - 1) / T;
+      V v[BP][C];
+#pragma unroll
+      for (int b = 0; b < BP; ++b) {
+        const int q = tid + b * T;
+        if (PM % T == 0 || q < PM) {
+          const int n2 = cx.rank * PM + q;
+#pragma unroll
+          for (int k1 = 0; k1 < C; ++k1) v[b][k1] = cx.P[pad(tslot(k1, n2))];
+#pragma unroll
+          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+          dft<C, -1>(v[b]);
+#pragma unroll
+          for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
+        }
+      }
+      __syncthreads();
     }
   }
 
@@ -628,7 +667,12 @@ struct Engine {
       if (keep_p) P[s] = mk<V>(p, (R)0);
       X[s] = raman ? x : cscale(x, p);
     };
-    inv(cx, X, rdXs, e1, false);  // the next exchange is a forward cross pass
+    // The P buffers are free here (their last use, the Raman inverse or an energy
+    // of the previous step, ended before a cluster barrier), so this inverse exchanges
+    // through them and leaves the exchange buffers W untouched; W was last read by the
+    // local passes of the previous forward transform, before the barrier of this
+    // inverse, so the next forward cross pass needs no barrier of its own to free W.
+    inv_via_p(cx, X, rdXs, e1);
     double energy = 0.0;
     if (want_e) energy = simpson_energy(cx, g, P);
     if (raman) {
@@ -636,7 +680,7 @@ struct Engine {
       const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
       auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
       auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
-      fwd(cx, P, rdPt, wrP, false);
+      fwd(cx, P, rdPt, wrP, false, false);
 #if GNLSE_RAMAN_SPLIT
       // spectral product and time-domain combination as separate passes over
       // this CTA's slice (fewer live registers in the transform passes)
@@ -663,7 +707,7 @@ struct Engine {
 #endif
     }
     auto wrX = [&](int, int l, V v) { X[pad(l)] = v; };
-    fwd(cx, X, rdXt, wrX, false);
+    fwd(cx, X, rdXt, wrX, false, raman);  // without Raman, W is still free (see above)
     return energy;
   }
 
