@@ -36,9 +36,6 @@
 #ifndef GNLSE_MINB_CAP
 #define GNLSE_MINB_CAP 16
 #endif
-#ifndef GNLSE_RAMAN_SPLIT
-#define GNLSE_RAMAN_SPLIT 0
-#endif
 // points each thread holds per pass (the radix is set in gnlse_twiddle.h)
 #ifndef GNLSE_PPT
 #define GNLSE_PPT 16
@@ -643,14 +640,7 @@ struct Engine {
   // |x|^2, on exit X holds G+(x R(x)) (spectral).  The transforms carry only
   // light per-element work in their first / last passes; with want_e the
   // Simpson energy (nJ) of x is returned.
-#ifndef GNLSE_NL_NOINLINE
-#define GNLSE_NL_NOINLINE 0
-#endif
-#if GNLSE_NL_NOINLINE
-  static __device__ __noinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
-#else
   static __device__ __forceinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
-#endif
     const R invN = (R)(1.0 / (double)N);
     const bool raman = g.raman != 0;
     V* X = cx.X;
@@ -681,21 +671,6 @@ struct Engine {
       auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
       auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
       fwd(cx, P, rdPt, wrP, false, false);
-#if GNLSE_RAMAN_SPLIT
-      // spectral product and time-domain combination as separate passes over
-      // this CTA's slice (fewer live registers in the transform passes)
-      for (int l = threadIdx.x; l < M; l += T) P[pad(l)] = cmul(P[pad(l)], __ldg(&Hp[cx.rank * M + l]));
-      __syncthreads();
-      auto rdPs = [&](int, int l) -> V { return P[pad(l)]; };
-      auto wrPt = [&](int n1, int n2, V v) { P[pad(tslot(n1, n2))] = v; };
-      inv(cx, P, rdPs, wrPt, false);
-      for (int l = threadIdx.x; l < M; l += T) {
-        const V x = X[pad(l)], conv = P[pad(l)];
-        const R p = cabs2(x);
-        X[pad(l)] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
-      }
-      __syncthreads();
-#else
       auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
       auto e3 = [&](int n1, int n2, V conv) {
         const int s = pad(tslot(n1, n2));
@@ -704,7 +679,6 @@ struct Engine {
         X[s] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
       };
       inv(cx, P, rdPH, e3, false);
-#endif
     }
     auto wrX = [&](int, int l, V v) { X[pad(l)] = v; };
     fwd(cx, X, rdXt, wrX, false, raman);  // without Raman, W is still free (see above)
