@@ -33,7 +33,7 @@ WORKLOAD = "sc_ensemble_256_ragged_2^12-2^14_ark4ip_1e-6"
 L2_FLUSH_BYTES = 256 << 20
 # dram__bytes_read.sum + dram__bytes_write.sum per ARK4IP attempt of one member, from
 # one ncu capture per class (profiles/); used to scale the dominant launch's traffic
-DRAM_BYTES_PER_ATTEMPT = {("mixed", 11, 8): 1.2483e9 / 530}
+DRAM_BYTES_PER_ATTEMPT = {("mixed", 11, 8): 1.4263e9 / 530}
 
 
 def parse():
