@@ -769,7 +769,8 @@ struct Engine {
   // and cis(t), |t| <= pi/1024, from its Taylor series in double-float, and
   // square the result for E2.
   static __device__ __noinline__ void exp_table(const Ctx& cx, const GridDev& g, double hh, SV* E1, SV* E2) {
-    const double mag = exp(-0.5 * g.alpha * hh);
+    // the attenuation factor is 1 for a lossless fibre (skips an FP64 exp per thread)
+    const double mag = g.alpha != 0.0 ? exp(-0.5 * g.alpha * hh) : 1.0;
     const int base = cx.rank * M;
     if constexpr (XS) {
       const float4* tab = (const float4*)g.cis_df;
@@ -811,7 +812,7 @@ struct Engine {
         E1[a] = mk<V>((R)mag * c, (R)mag * s);
         if (E2) {
           const double ph2 = g.beta[a] * (2.0 * hh);
-          const double mag2 = exp(-g.alpha * hh);
+          const double mag2 = g.alpha != 0.0 ? exp(-g.alpha * hh) : 1.0;
           if constexpr (sizeof(R) == 4) {
             const double TWO_PI = 6.283185307179586476925286766559;
             sincosf((float)(ph2 - TWO_PI * rint(ph2 * (1.0 / TWO_PI))), &s, &c);
