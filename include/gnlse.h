@@ -60,10 +60,14 @@ enum {
   GNLSE_RUNNING = 8          /* instance not finished (attempt budget reached) */
 };
 
-/* Methods: Solver.rk4ip with the fixed-step or the adaptive (step-doubling) driver, and
- * Solver.ss_sym_rk4 (pyofss/modules/solver.py:330-337: linear half step, classical RK4 on
- * the nonlinear term, linear half step) with the fixed-step driver. */
-enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2 };
+/* Methods: Solver.rk4ip with the fixed-step or the adaptive (step-doubling) driver;
+ * with the fixed-step driver, Solver.ss_sym_rk4 (pyofss/modules/solver.py:330-337: linear
+ * half step, classical RK4 on the nonlinear term, linear half step) and
+ * Solver.ss_symmetric (solver.py:267-275: linear half step, exponential nonlinear step
+ * evaluated with the unpropagated field, linear half step; not with self-steepening,
+ * whose exponent in the reference divides by the field).  Neither split step runs with
+ * gain (GNLSE_UNSUPPORTED). */
+enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2, GNLSE_SS_SYMMETRIC = 3 };
 /* precision: GNLSE_FP32 complex64 throughout (fields complex64);
  * GNLSE_FP64 complex128 throughout (fields complex128);
  * GNLSE_MIXED complex64 transforms and nonlinear evaluations with the
@@ -96,7 +100,7 @@ typedef struct {
 /* One propagation (one field through one fibre). */
 typedef struct {
   int32_t grid;               /* index into the grid array */
-  int32_t method;             /* GNLSE_RK4IP / GNLSE_SS_SYM_RK4 (fixed step), GNLSE_ARK4IP (adaptive) */
+  int32_t method;             /* GNLSE_RK4IP / GNLSE_SS_SYM_RK4 / GNLSE_SS_SYMMETRIC (fixed step), GNLSE_ARK4IP */
   int32_t total_steps;        /* Fibre total_steps */
   int32_t traces;             /* Fibre traces (>= 1) */
   int32_t max_traces;         /* trace slots reserved for this instance (0: none) */

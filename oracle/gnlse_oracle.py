@@ -268,6 +268,25 @@ class Nonlinear:
         # default_f (nonlinearity.py:266-267)
         return self.factor * np.abs(A) ** 2 * A
 
+    def exp_non(self, A, h, B):
+        """Exponential nonlinear step of the split-step methods."""
+        if self.use_all:
+            # default_exp_f_all (nonlinearity.py:209-221)
+            term_spm = np.abs(A) ** 2
+            convolution = ifft(self.h_R * fft(term_spm))
+            term_all = (1.0 - self.f_R) * term_spm + self.f_R * convolution
+            with np.errstate(divide="ignore", invalid="ignore"):
+                inv_b = np.where(np.abs(B) > 1e-15, self.ss_factor / B, 0.0)
+            term_ss_all = inv_b * ifft(self.omega * fft(term_all * A))
+            return np.exp(h * self.factor * (term_all + term_ss_all)) * B
+        if self.ss_on:
+            # default_exp_f_with_ss (nonlinearity.py:230-234)
+            term_spm = np.abs(A) ** 2
+            term_ss = (self.ss_factor / B) * ifft(self.omega * fft(term_spm * A))
+            return np.exp(h * self.factor * (term_spm + term_ss)) * B
+        # default_exp_f (nonlinearity.py:269-270)
+        return np.exp(h * self.factor * np.abs(A) ** 2) * B
+
 
 class Gain:
     """``Amplifier`` simple saturable gain with Lorentzian profile (amplifier.py:42-158)."""
@@ -367,6 +386,14 @@ class Propagator:
         k3 = h * f(A + k2)
         return A + (k0 + 2.0 * (k1 + k2) + k3) / 6.0
 
+    def ss_symmetric(self, A, h):
+        """``Solver.ss_symmetric`` (solver.py:267-275): linear half step, exponential
+        nonlinear step evaluated with the unpropagated field, linear half step."""
+        self.evals += 1
+        A_L = self.linear(A, 0.5 * h)
+        A_N = self.nl.exp_non(A, h, A_L)
+        return self.linear(A_N, 0.5 * h)
+
     def ss_sym_rk4(self, A, h):
         """``Solver.ss_sym_rk4`` (solver.py:330-337): linear half step, classical RK4 on
         the nonlinear term, linear half step."""
@@ -381,7 +408,7 @@ class Propagator:
         zs = np.linspace(0.0, self.length, total_steps + 1)
         storage_step = int(total_steps / traces)
         trace_z, trace_A = [], []
-        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4}[method]
+        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric}[method]
         for i, z in enumerate(zs[:-1]):
             A = step(A, h)
             if traces != 1 and i % storage_step == 0:

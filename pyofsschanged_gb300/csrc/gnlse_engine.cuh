@@ -961,6 +961,88 @@ struct Engine {
     __syncthreads();
   }
 
+  // One step of Solver.ss_symmetric (solver.py:267-275) without self-steepening:
+  //   S_L = E S                                   (linear half step, E = exp(hD/2))
+  //   B = G-(S_L)/N, a = G-(S)/N                  (time domain; B kept in global Bt)
+  //   t = (1 - fR)|a|^2 + fR G-(Hp G+(|a|^2))     (or |a|^2; default_exp_f[_all],
+  //                                                 nonlinearity.py:209-221,269-270)
+  //   A_N = exp(i gamma h t) B ;  S' = E G+(A_N)  (linear half step)
+  // computed as S' = E (S_L + G+((exp(i gamma h t) - 1) B)), which keeps the
+  // propagation state's precision when the nonlinear phase per step is small.
+  static __device__ __forceinline__ void ss_symmetric_step(const Ctx& cx, const GridDev& g, const SV* S, SV* Sh,
+                                                        V* Bt, const SV* E, double h) {
+    const R invN = (R)(1.0 / (double)N);
+    const int base = cx.rank * M;
+    V* X = cx.X;
+    V* P = cx.P;
+    {  // S_L = E S -> Sh
+      struct In { SL e, s; };
+      each_slot<4, In>([&](int l) { return In{lds(E, base + l), lds(S, base + l)}; },
+                       [&](int l, const In& r) {
+                         if constexpr (XS) {
+                           dfc_store(Sh, base + l, dfc_mul(r.e, r.s));
+                         } else {
+                           Sh[base + l] = cmul(r.e, r.s);
+                         }
+                       });
+      __syncthreads();
+    }
+    auto rdSh = [&](int o, int l) -> V { return ldv(Sh, o * M + l); };
+    auto wrB = [&](int n1, int n2, V v) { Bt[n1 * M + n2] = cscale(v, invN); };
+    inv(cx, X, rdSh, wrB);  // B = G-(S_L)/N
+    auto rdS = [&](int o, int l) -> V { return ldv(S, o * M + l); };
+    auto e1 = [&](int n1, int n2, V v) {
+      const int sl = pad(tslot(n1, n2));
+      const V x = cscale(v, invN);
+      X[sl] = x;
+      P[sl] = mk<V>(cabs2(x), (R)0);
+    };
+    inv(cx, X, rdS, e1);  // a = G-(S)/N, |a|^2
+    if (g.raman) {
+      const V* Hp = (const V*)g.Hp;
+      const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
+      auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
+      auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
+      fwd(cx, P, rdPt, wrP);
+      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
+      auto e3 = [&](int n1, int n2, V conv) {
+        const int sl = pad(tslot(n1, n2));
+        P[sl] = mk<V>(f1 * cabs2(X[sl]) + fR * conv.x, fR * conv.y);
+      };
+      inv(cx, P, rdPH, e3);
+    }
+    __syncthreads();
+    // Delta = (exp(i gamma h t) - 1) B in X: exp(x + iy) - 1 = expm1(x) cos y - 2 sin^2(y/2) + i e^x sin y
+    const double gh = h * (double)__ldg((const R*)g.Kr);  // gamma h (Kr = gamma without self-steepening)
+    for (int l = threadIdx.x; l < M; l += T) {
+      const V t = P[pad(l)];
+      const V b = Bt[tsample(cx.rank, l)];
+      const R px = (R)(-gh) * t.y, py = (R)gh * t.x;
+      R sn, cs;
+      if constexpr (sizeof(R) == 4) {
+        sincosf(py, &sn, &cs);
+      } else {
+        sincos(py, &sn, &cs);
+      }
+      const R hs = sizeof(R) == 4 ? sinf(0.5f * (float)py) : (R)sin(0.5 * (double)py);
+      const R em1 = sizeof(R) == 4 ? expm1f((float)px) : (R)expm1((double)px);
+      const V ephi = mk<V>(em1 * cs - (R)2 * hs * hs, (em1 + (R)1) * sn);
+      X[pad(l)] = cmul(ephi, b);
+    }
+    __syncthreads();
+    // S' = E (S_L + G+(Delta))
+    auto rdXt = [&](int n1, int n2) -> V { return X[pad(tslot(n1, n2))]; };
+    auto wrS = [&](int, int l, V v) {
+      const int a = base + l;
+      if constexpr (XS) {
+        dfc_store(Sh, a, dfc_mul(dfc_load(E, a), dfc_add_f(dfc_load(Sh, a), v)));
+      } else {
+        Sh[a] = cmul(E[a], cadd(Sh[a], v));
+      }
+    };
+    fwd(cx, X, rdXt, wrS);
+  }
+
   // dst = E dst over this CTA's slice: the linear half steps of the split-step method
   static __device__ __noinline__ void scale_state(const Ctx& cx, SV* dst, const SV* E) {
     const int base = cx.rank * M;
@@ -1099,6 +1181,32 @@ struct Engine {
     __syncthreads();
   }
 
+  // Fixed-step driver after a step (stepper.py:164-221): z from the linspace mesh,
+  // the new state becomes current, traces every int(steps/traces) steps.
+  static __device__ __forceinline__ void fixed_step_done(const Ctx& cx, const KParams& kp, Ctl& c, SV* base,
+                                                         double h) {
+    const InstDev& d = c.d;
+    InstState& st = c.st;
+    const double dz = d.length / d.total_steps;  // numpy linspace step of the z mesh
+    const int storage_step = d.traces > 0 ? d.total_steps / d.traces : 0;
+    const long long i = st.steps;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      st.attempts += 1;
+      st.sidx ^= 1;
+      st.accepted += 1;
+      st.steps += 1;
+      st.z = (st.steps == d.total_steps) ? d.length : (double)st.steps * dz;
+      if (st.steps >= d.total_steps) {
+        st.status = ST_OK;
+        st.phase = 2;
+      }
+    }
+    __syncthreads();
+    if (d.traces != 1 && storage_step > 0 && (i % storage_step) == 0)
+      store_trace(cx, kp, c, base + (long long)st.sidx * N, (double)i * dz + h);
+  }
+
   // The whole propagation of one instance.  Every CTA of a cluster evaluates
   // the same control decisions from the same cluster-reduced values, so all
   // CTAs follow one path.  An attempt is a loop over its nonlinear
@@ -1183,9 +1291,22 @@ struct Engine {
     // term (the RK4IP stage algebra with the exp(hD/2) factors replaced by an exact 1,
     // table 6), result <- E result, E = exp(hD/2) (table 7)
     const bool ssrk = d.method == 2;
+    const bool sssym = d.method == 3;  // Solver.ss_symmetric, ss_symmetric_step
     if (st.phase == 1 && !adaptive) {
       exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
       if (ssrk) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
+    }
+
+    // Solver.ss_symmetric: a step loop of its own, so that the main loop below keeps
+    // no call of its step function (its register allocation would suffer)
+    while (sssym && st.phase == 1 && budget > 0) {
+      const double h = d.length / d.total_steps;
+      const int sidx = st.sidx;
+      ss_symmetric_step(cx, g, base + (long long)sidx * N, base + (long long)(sidx ^ 1) * N,
+                        reinterpret_cast<V*>(base + 2 * N), base + 7 * N, h);
+      if (threadIdx.x == 0) st.evals += 1;
+      budget -= 1;
+      fixed_step_done(cx, kp, c, base, h);
     }
 
     while (st.phase == 1 && budget > 0) {
@@ -1291,25 +1412,7 @@ struct Engine {
       budget -= 1;
 
       if (!adaptive) {
-        // Fixed-step driver (stepper.py:164-221)
-        const double dz = d.length / d.total_steps;  // numpy linspace step of the z mesh
-        const int storage_step = d.traces > 0 ? d.total_steps / d.traces : 0;
-        const long long i = st.steps;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          st.attempts += 1;
-          st.sidx ^= 1;
-          st.accepted += 1;
-          st.steps += 1;
-          st.z = (st.steps == d.total_steps) ? d.length : (double)st.steps * dz;
-          if (st.steps >= d.total_steps) {
-            st.status = ST_OK;
-            st.phase = 2;
-          }
-        }
-        __syncthreads();
-        if (d.traces != 1 && storage_step > 0 && (i % storage_step) == 0)
-          store_trace(cx, kp, c, base + (long long)st.sidx * N, (double)i * dz + h);
+        fixed_step_done(cx, kp, c, base, h);
         continue;
       }
 

@@ -117,8 +117,9 @@ class Fibre:
         m = method.lower()
         if m.startswith("cuda_"):
             m = m[5:]
-        if m not in ("rk4ip", "ark4ip", "ss_sym_rk4"):
-            raise NotImplementedError(f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4")
+        if m not in ("rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric"):
+            raise NotImplementedError(
+                f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4 / ss_symmetric")
         if sim_type not in (None, "default"):
             raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
         if raman_scattering and not use_all:
