@@ -4,9 +4,10 @@ Constructor arguments are those of ``pyofss.modules.fibre.Fibre``
 (pyofss/modules/fibre.py:74-134); calling the module with ``(domain, field)``
 propagates the field through the fibre and returns it, as
 ``Fibre.__call__`` does (fibre.py:136-148).  ``method`` selects the engine
-path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps) or
+path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps),
 ``"cuda_ark4ip"`` / ``"ark4ip"`` (adaptive step doubling with tolerance
-``local_error``).  ``precision`` selects ``"mixed"`` (default: complex64
+``local_error``), or the fixed-step split-step methods ``"ss_sym_rk4"`` and
+``"ss_symmetric"`` (pyofss/modules/solver.py:267-275,330-337).  ``precision`` selects ``"mixed"`` (default: complex64
 transforms with a double-float propagation state), ``"fp32"`` (complex64
 throughout) or ``"fp64"`` (complex128 throughout).  The stepper exceptions of
 pyofss/modules/stepper.py:33-47 are raised with the same names.
