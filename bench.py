@@ -31,6 +31,7 @@ METRIC = "GNLSE ensemble solves/s on 1 GB300 (fused vs plain, <=1e-4 rel spectra
 UNIT = "solves/s"
 WORKLOAD = "sc_ensemble_256_ragged_2^12-2^14_ark4ip_1e-6"
 L2_FLUSH_BYTES = 256 << 20
+ENSEMBLE_SEED = 20261203  # sc_ensemble's default seed: rank 0 is the reference ensemble
 # dram__bytes_read.sum + dram__bytes_write.sum per ARK4IP attempt of one member, from
 # one ncu capture per class (profiles/); used to scale the dominant launch's traffic
 DRAM_BYTES_PER_ATTEMPT = {("mixed", 11, 8): 1.4263e9 / 530}
@@ -226,7 +227,9 @@ def run_ours(a):
     from pyofsschanged_gb300.engine import Plan
     from pyofsschanged_gb300.ensemble import ensemble_plan_inputs, sc_ensemble
 
-    members, domains, fields = sc_ensemble(a.members)
+    # each rank propagates its own shard of a world x members ensemble (seeded per
+    # rank; weak scaling, no collective during propagation)
+    members, domains, fields = sc_ensemble(a.members, seed=ENSEMBLE_SEED + rank)
     cluster = {int(k): int(v) for k, v in (kv.split(":") for kv in a.cluster.split(",") if kv)}
     grids, inst = ensemble_plan_inputs(members, domains, cluster=cluster)
     tuned = None
@@ -304,6 +307,15 @@ def run_ours(a):
     assert all(s["status"] == 0 and s["finished"] for s in stats), "a member did not finish"
     ms_step = ms_total / a.steps
     value = world * a.members * a.steps / (ms_total * 1e-3)
+
+    # ensemble coherence |g12| over every rank's members (untimed): one all-reduce of the
+    # spectral sums, the spectra stay on their ranks
+    from pyofsschanged_gb300.ensemble import coherence_g12, coherence_g12_distributed, common_spectra
+    spectra = common_spectra([x.cpu().numpy().astype(complex) for x in plan.unpack(work)])
+    g12 = coherence_g12_distributed(spectra) if world > 1 else coherence_g12(spectra)
+    power = np.sum(np.abs(spectra) ** 2, axis=0)
+    coherence = {"members": world * a.members,
+                 "g12_power_weighted": float(np.sum(g12 * power) / np.sum(power))}
 
     # roofline of the dominant launch: the class launch with the most algorithmic
     # bytes (RK4IP evaluations x 2 x N x element size), timed by its own CUDA events
@@ -433,7 +445,7 @@ def run_ours(a):
                        "class_sm_us_per_attempt": tuned,
                        "evals_per_step": evals},
             "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
-            "gpu_launches": launches, "accuracy_vs_fp64": acc, "plain": plain,
+            "gpu_launches": launches, "accuracy_vs_fp64": acc, "plain": plain, "coherence": coherence,
             "class_ms": {f"m2^{lm}_c{c}_n{cnt}": statistics.mean(st[k][3] for st in class_ms)
                          for k, (lm, c, cnt, _) in enumerate(class_ms[0])}}
     if rank == 0:

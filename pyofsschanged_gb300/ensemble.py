@@ -113,6 +113,52 @@ def coherence_g12(spectra):
         return np.where(den > 0, num / den, 0.0)
 
 
+def shard(members, rank, world):
+    """Member indices of one rank: a contiguous block of the members sorted by
+    estimated cost (N log N x expected attempts), cut so every rank gets about the
+    same total cost.  Members are independent, so the ranks propagate their shards
+    with no collective; only ensemble statistics are reduced afterwards."""
+    cost = [m.n * math.log2(m.n) * expected_attempts(m) for m in members]
+    order = sorted(range(len(members)), key=lambda i: -cost[i])
+    total = sum(cost)
+    out, acc, r = [[] for _ in range(world)], 0.0, 0
+    for i in order:
+        # advance to the next rank once this one holds its share (keep >= 1 member each)
+        while r < world - 1 and acc >= total * (r + 1) / world and out[r]:
+            r += 1
+        out[r].append(i)
+        acc += cost[i]
+    return sorted(out[rank])
+
+
+def coherence_partial(spectra):
+    """Per-rank sums for coherence_g12: (sum_i A_i, sum_i |A_i|^2, count)."""
+    spectra = np.asarray(spectra)
+    return spectra.sum(axis=0), (np.abs(spectra) ** 2).sum(axis=0), spectra.shape[0]
+
+
+def coherence_from_sums(s, p, n):
+    """|g12| from the ensemble sums of coherence_partial, all-reduced over ranks."""
+    num = np.abs(np.abs(s) ** 2 - p) / (n * (n - 1))
+    den = p / n
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(den > 0, num / den, 0.0)
+
+
+def coherence_g12_distributed(spectra, group=None):
+    """coherence_g12 over the union of every rank's spectra: one all-reduce of the
+    sums (torch.distributed, any backend), so the spectra themselves never move."""
+    import torch
+    import torch.distributed as dist
+    s, p, n = coherence_partial(spectra)
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    buf = torch.tensor(np.concatenate([s.real, s.imag, p, [float(n)]]), dtype=torch.float64, device=dev)
+    dist.all_reduce(buf, group=group)
+    b = buf.cpu().numpy()
+    k = len(p)
+    return coherence_from_sums(b[:k] + 1j * b[k:2 * k], b[2 * k:3 * k], b[-1])
+
+
 def common_spectra(fields, sizes_min=4096):
     """Spectra of members on the coarsest grid's frequency points (FFT order).
 
