@@ -15,6 +15,8 @@
  *                       Nonlinearity.__call__ (pyofss/modules/nonlinearity.py:160-185),
  *                       Amplifier.set_domain / spectal_filtration_array
  *                       (pyofss/modules/amplifier.py:110-147),
+ *                       Amplifier2LevelModel.set_domain and its tables
+ *                       (amplifier.py:247-344),
  *                       Stepper.__init__ (pyofss/modules/stepper.py:87-145)
  *   gnlse_propagate     Fibre.__call__ (pyofss/modules/fibre.py:136-148) ->
  *                       Stepper.__call__ (stepper.py:147-156) ->
@@ -45,7 +47,7 @@
 extern "C" {
 #endif
 
-#define GNLSE_ABI_VERSION 1
+#define GNLSE_ABI_VERSION 2
 
 /* status codes (per call and per instance) */
 enum {
@@ -66,7 +68,7 @@ enum {
  * Solver.ss_symmetric (solver.py:267-275: linear half step, exponential nonlinear step
  * evaluated with the unpropagated field, linear half step; not with self-steepening,
  * whose exponent in the reference divides by the field).  Neither split step runs with
- * gain (GNLSE_UNSUPPORTED). */
+ * gain or the Yb model (GNLSE_UNSUPPORTED). */
 enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2, GNLSE_SS_SYMMETRIC = 3 };
 /* precision: GNLSE_FP32 complex64 throughout (fields complex64);
  * GNLSE_FP64 complex128 throughout (fields complex128);
@@ -95,6 +97,24 @@ typedef struct {
   double E_sat;               /* nJ */
   double gain_length;         /* amplifier length = fibre length, km */
   const double* gain_profile; /* [n] spectral gain profile (FFT order) */
+  /* Yb two-level gain, Amplifier2LevelModel (pyofss/modules/amplifier.py:178-379);
+   * excludes gain_on.  Every linear-operator call of the solver sets the inversion
+   *   n2 = (yb_pump_ratio Pp / yb_pump_sat + sum_k yb_w_ratio[k] |X_k|^2)
+   *      / (1 + Pp / yb_pump_sat + sum_k yb_w_sat[k] |X_k|^2)
+   * from the spectrum X = n fft(x) (pyofss fft) of its argument x, applies the gain
+   * exp(500 h (n2 yb_alpha[k] - yb_eta[k])) over the call's step h (km) and advances
+   * the pump power Pp <- Pp exp(1000 h (n2 yb_pump_alpha - yb_pump_eta)). */
+  int32_t yb_on;
+  int32_t pad1;
+  double yb_pump_w;           /* Pp_0: pump power entering the fibre, W */
+  double yb_pump_sat;         /* Psat_p, W */
+  double yb_pump_ratio;       /* sigma12_p / (sigma12_p + sigma21_p) */
+  double yb_pump_alpha;       /* alpha_p N, 1/m */
+  double yb_pump_eta;         /* eta_p, 1/m */
+  const double* yb_alpha;     /* [n] alpha_s N = (sigma12_s + sigma21_s) rho_s N, 1/m (FFT order) */
+  const double* yb_eta;       /* [n] eta_s = sigma12_s rho_s N, 1/m (FFT order) */
+  const double* yb_w_ratio;   /* [n] ratio_s / Psat_s * dt / (n Tr), 0 where NaN (FFT order) */
+  const double* yb_w_sat;     /* [n] 1 / Psat_s * dt / (n Tr), 0 where NaN (FFT order) */
 } gnlse_grid_desc;
 
 /* One propagation (one field through one fibre). */
@@ -126,6 +146,7 @@ typedef struct {
   int32_t ntraces;            /* traces written */
   int32_t trace_overflow;     /* 1 if traces were dropped for lack of slots */
   int32_t finished;           /* 1 once the output field has been written */
+  double pump_w;              /* Yb gain: pump power reached (Amplifier2LevelModel.Pp), W */
 } gnlse_stats;
 
 typedef struct gnlse_plan gnlse_plan;
@@ -212,7 +233,7 @@ int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
  * state live in one file-scope device array of 585 KiB that every GPU loading
  * the library keeps until exit; the caller passes the grid's host tables, the
  * instance description (max_traces must be 0) and the field d_field (device,
- * in place).  Larger grids return GNLSE_UNSUPPORTED.  All calls share the
+ * in place).  Larger grids and the Yb model return GNLSE_UNSUPPORTED.  All calls share the
  * array: calls whose GPU work overlaps (other streams or threads) race and
  * must be serialised by the caller.  The first call on each device looks up
  * the array's address; make it before any stream capture.  The call waits for

@@ -21,6 +21,7 @@ time-domain formulation of:
 * ``Amplifier.factor`` with the Lorentzian gain profile
   (``pyofss/modules/amplifier.py:110-158``) and Simpson energy
   (``pyofss/field.py:161-172``);
+* the Yb two-level gain ``Amplifier2LevelModel`` (``pyofss/modules/amplifier.py:178-379``);
 * ``Solver.rk4ip`` (``pyofss/modules/solver.py:339-354``);
 * ``Stepper.standard_stepper`` / ``adaptive_stepper`` / ``relative_local_error``
   (``pyofss/modules/stepper.py:164-221,231-376``).
@@ -309,6 +310,86 @@ class Gain:
         return g0 / (1.0 + E / self.E_sat) * self.profile
 
 
+def yb_cross_sections(grid, path):
+    """``Amplifier2LevelModel.interpolate_sigma_s`` (amplifier.py:234-245).
+
+    The table (wavelength m, sigma_12 m^2, sigma_21 m^2, comma separated) is read as
+    pandas does with its default header inference: the first line names the columns
+    and is not data.  Cubic interpolating splines in (nm, 1e27 sigma), zero outside
+    the table, evaluated at the grid's wavelengths (natural order).
+    """
+    from scipy.interpolate import InterpolatedUnivariateSpline as IUS
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    tab = np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]])
+    s12 = IUS(tab[:, 0] * 1e9, tab[:, 1] * 1e27, ext=1)(grid.Lambda) * 1e-27
+    s21 = IUS(tab[:, 0] * 1e9, tab[:, 2] * 1e27, ext=1)(grid.Lambda) * 1e-27
+    return s12, s21
+
+
+class YbGain:
+    """``Amplifier2LevelModel`` (amplifier.py:178-344): Yb two-level rate-equation gain.
+
+    ``sigma12_s``/``sigma21_s`` are the signal cross sections on the grid (natural
+    order, m^2).  Each ``factor`` call sets the inversion from the argument's
+    spectral power and advances the pump power (``update_Pp``), as the reference
+    does on every linear-operator call.
+    """
+
+    H_P = 6.62e-34            # amplifier.py:201-211
+    T_LIFE = 850.0e-6         # s
+    A_CORE = 3.0e-6           # m
+    B_CLAD = 60.0e-6          # m
+    NA = 0.13
+    LAMBDA_P = 976.0          # nm
+    SIGMA12_P = 2.5e-24       # m^2 (amplifier.py:217-218)
+    SIGMA21_P = 2.44e-24
+
+    def __init__(self, grid, Pp_0, N, Rr, sigma12_s, sigma21_s):
+        a = self.A_CORE
+        self.grid = grid
+        self.N = N * 1e25 * np.pi * a ** 2
+        self.Pp = Pp_0
+        self.Tr = 1.0 / Rr
+        s12, s21 = np.asarray(sigma12_s, float), np.asarray(sigma21_s, float)
+        # rho_s, rho_p (amplifier.py:255-273)
+        V = (2.0 * np.pi / grid.Lambda) * a * self.NA * 1e9
+        omega_s = a * (0.616 + 1.66 / pow(V, 1.5) + 0.987 / pow(V, 6.0))
+        gamma_s = 1.0 - np.exp(-2.0 * a ** 2 / (omega_s * omega_s))
+        rho_s = gamma_s / (np.pi * a ** 2)
+        rho_p = (a ** 2) / (self.B_CLAD ** 2) / (np.pi * a ** 2)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            # Psat, eta, alpha, ratio (amplifier.py:275-344)
+            self.Psat_s = (self.H_P * grid.nu * 1e12) / (self.T_LIFE * (s12 + s21) * rho_s)
+            self.ratio_s = s12 / (s12 + s21)
+        sp = self.SIGMA12_P + self.SIGMA21_P
+        self.Psat_p = (self.H_P * lambda_to_nu(self.LAMBDA_P) * 1e12) / (self.T_LIFE * sp * rho_p)
+        self.eta_s = s12 * rho_s * self.N
+        self.eta_p = self.SIGMA12_P * rho_p * self.N
+        self.alpha_s = (s12 + s21) * rho_s
+        self.alpha_p = sp * rho_p
+        self.ratio_p = self.SIGMA12_P / sp
+
+    def calculate_N2(self, Ps):
+        """amplifier.py:346-353; terms that are NaN (zero cross sections) are left out."""
+        with np.errstate(divide="ignore", invalid="ignore"):
+            x = self.ratio_s * Ps / self.Psat_s
+            y = Ps / self.Psat_s
+        num = self.ratio_p * self.Pp / self.Psat_p + np.sum(x[~np.isnan(x)])
+        den = 1 + self.Pp / self.Psat_p + np.sum(y[~np.isnan(y)])
+        return (num / den) * self.N
+
+    def factor(self, A, h):
+        """amplifier.py:366-379: the spectral power (natural order, like the tables)
+        scaled to the average power at the repetition rate; the gain exponent is
+        returned in FFT order."""
+        N2 = self.calculate_N2(spectral_power(A) * len(A) * self.grid.dt / self.Tr)
+        g_s = self.alpha_s * N2 - self.eta_s
+        g_p = self.alpha_p * N2 - self.eta_p
+        self.Pp = self.Pp * np.exp(g_p * h * 1e3)
+        return fftshift(g_s * h * 1e3 / 2)
+
+
 # ----------------------------------------------------------------------------
 # Propagation
 # ----------------------------------------------------------------------------
@@ -344,13 +425,17 @@ class Propagator:
 
     def __init__(self, grid, length, beta=None, alpha=None, gamma=0.0, self_steepening=False,
                  use_all=False, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18, centre_omega=None,
-                 small_signal_gain=None, E_sat=None, lamb0=None, bandwidth=None):
+                 small_signal_gain=None, E_sat=None, lamb0=None, bandwidth=None,
+                 use_Yb_model=False, Pp_0=None, N=None, Rr=None, yb_cross_sections=None):
         self.grid = grid
         self.length = length
         self.factor = linear_factor(grid, beta, alpha, centre_omega)
         self.nl = Nonlinear(grid, gamma, self_steepening, use_all, tau_1, tau_2, f_R)
         self.gain = None
-        if small_signal_gain is not None and E_sat is not None:
+        if use_Yb_model:  # fibre.py:97-103: the Yb model replaces the saturable amplifier
+            s12, s21 = yb_cross_sections
+            self.gain = YbGain(grid, Pp_0, N, Rr, s12, s21)
+        elif small_signal_gain is not None and E_sat is not None:
             self.gain = Gain(grid, small_signal_gain, E_sat, length, lamb0, bandwidth)
         self.fft_count = 0
         self.evals = 0

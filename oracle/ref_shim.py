@@ -12,8 +12,9 @@ the reference, this shim:
   ``scipy.log10``, ``scipy.exp``, ``scipy.sqrt``, ``scipy.log``,
   ``scipy.integrate.simps``) and ``collections.Iterable``;
 * registers empty stand-ins for optional modules the reference imports at
-  module level but never uses on the CPU propagation path (pandas, matplotlib,
-  pyopencl, reikna, pynvml, unittest2);
+  module level but never uses on the CPU propagation path (matplotlib,
+  pyopencl, reikna, pynvml, unittest2), and, when pandas is absent, a
+  ``read_csv`` for the numeric tables the Yb gain model reads;
 * pre-registers ``pyofss`` as a package object with ``__path__`` so that
   ``pyofss/__init__.py`` (which pulls in the plotter and OpenCL modules) is not
   executed.
@@ -56,6 +57,40 @@ class _Stub(types.ModuleType):
         return (object,)
 
 
+class _Frame:
+    """The part of a pandas DataFrame the reference uses: ``columns`` and column lookup."""
+
+    def __init__(self, names, data):
+        self.columns = names
+        self._cols = {name: data[:, i] for i, name in enumerate(names)}
+
+    def __getitem__(self, name):
+        return self._cols[name]
+
+
+def _mini_pandas():
+    """``pandas.read_csv`` for the reference's numeric data tables, used by
+    ``Amplifier2LevelModel.interpolate_sigma_s`` (pyofss/modules/amplifier.py:234-245).
+
+    As pandas does with its default ``header="infer"``, the first line becomes the
+    column names, so the first data row of a headerless table is not data; with
+    ``header=None`` every line is data and the columns are 0, 1, ...  Values are
+    parsed with Python's correctly rounded ``float``.
+    """
+    mod = types.ModuleType("pandas")
+
+    def read_csv(path, delimiter=",", header="infer", **_):
+        with open(path) as f:
+            lines = [ln for ln in f.read().splitlines() if ln.strip()]
+        names = None if header is None else lines[0].split(delimiter)
+        rows = lines if header is None else lines[1:]
+        data = np.array([[float(x) for x in r.split(delimiter)] for r in rows])
+        return _Frame(list(range(data.shape[1])) if names is None else names, data)
+
+    mod.read_csv = read_csv
+    return mod
+
+
 def available():
     return os.path.isdir(os.path.join(REFERENCE_ROOT, "pyofss"))
 
@@ -83,7 +118,11 @@ def load():
     if not hasattr(collections, "Iterable"):
         collections.Iterable = collections.abc.Iterable
 
-    for mod in ("pandas", "matplotlib", "matplotlib.pyplot", "pyopencl",
+    try:
+        importlib.import_module("pandas")
+    except Exception:
+        sys.modules["pandas"] = _mini_pandas()
+    for mod in ("matplotlib", "matplotlib.pyplot", "pyopencl",
                 "pyopencl.array", "reikna", "reikna.cluda", "reikna.fft",
                 "pynvml", "unittest2", "tqdm"):
         if mod not in sys.modules:

@@ -41,6 +41,10 @@ class GridDesc(ct.Structure):
         ("nu", _dp), ("gain_on", ct.c_int32), ("pad0", ct.c_int32),
         ("gain_log", ct.c_double), ("E_sat", ct.c_double), ("gain_length", ct.c_double),
         ("gain_profile", _dp),
+        ("yb_on", ct.c_int32), ("pad1", ct.c_int32),
+        ("yb_pump_w", ct.c_double), ("yb_pump_sat", ct.c_double), ("yb_pump_ratio", ct.c_double),
+        ("yb_pump_alpha", ct.c_double), ("yb_pump_eta", ct.c_double),
+        ("yb_alpha", _dp), ("yb_eta", _dp), ("yb_w_ratio", _dp), ("yb_w_sat", _dp),
     ]
 
 
@@ -61,7 +65,7 @@ class Stats(ct.Structure):
         ("attempts", ct.c_int64), ("accepted", ct.c_int64), ("rejected", ct.c_int64),
         ("evals", ct.c_int64), ("steps", ct.c_int64),
         ("status", ct.c_int32), ("ntraces", ct.c_int32), ("trace_overflow", ct.c_int32),
-        ("finished", ct.c_int32),
+        ("finished", ct.c_int32), ("pump_w", ct.c_double),
     ]
 
     def as_dict(self):

@@ -72,6 +72,8 @@ struct GridHost {
   void* d_tw64 = nullptr;
   void* d_twl64 = nullptr;
   void* d_cis = nullptr;
+  void* d_lor2 = nullptr;
+  void* d_ybw = nullptr;
   void* d_twp = nullptr;
   void* d_twp64 = nullptr;
 };
@@ -181,7 +183,8 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   const int n = gd.n, C = gh.C, M = n / C;
   auto perm = [&](int a) { return (a % M) * C + a / M; };  // slot a = c*M + k2  <-  k = c + C*k2
   std::vector<double> beta(n), nu(n);
-  std::vector<R> Kr(n), lor, Hp;
+  std::vector<R> Kr(n), lor, lor2, Hp;
+  std::vector<double> ybw;
   std::vector<R> tw(2 * (size_t)n), twl(2 * (size_t)M);
   for (int a = 0; a < n; ++a) {
     const int k = perm(a);
@@ -201,6 +204,19 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   if (gd.gain_on) {
     lor.resize(n);
     for (int a = 0; a < n; ++a) lor[a] = (R)(gd.gain_profile ? gd.gain_profile[perm(a)] : 1.0);
+  }
+  const bool yb = gd.yb_on != 0;
+  if (yb) {  // Yb model: lor = alpha_s N, lor2 = eta_s, inversion weights in FP64
+    lor.resize(n);
+    lor2.resize(n);
+    ybw.resize(2 * (size_t)n);
+    for (int a = 0; a < n; ++a) {
+      const int k = perm(a);
+      lor[a] = (R)gd.yb_alpha[k];
+      lor2[a] = (R)gd.yb_eta[k];
+      ybw[2 * (size_t)a] = gd.yb_w_ratio[k];
+      ybw[2 * (size_t)a + 1] = gd.yb_w_sat[k];
+    }
   }
   // exp(+2 pi i j / n), argument formed in long double
   for (int j = 0; j < n; ++j) {
@@ -264,11 +280,15 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   if ((e = upload(p, Kr, &gh.d_Kr)) != cudaSuccess) return e;
   if ((e = upload(p, tw, &gh.d_tw)) != cudaSuccess) return e;
   if (raman && (e = upload(p, Hp, &gh.d_Hp)) != cudaSuccess) return e;
-  if (gd.gain_on && (e = upload(p, lor, &gh.d_lor)) != cudaSuccess) return e;
+  if ((gd.gain_on || yb) && (e = upload(p, lor, &gh.d_lor)) != cudaSuccess) return e;
+  if (yb && (e = upload(p, lor2, &gh.d_lor2)) != cudaSuccess) return e;
+  if (yb && (e = upload(p, ybw, &gh.d_ybw)) != cudaSuccess) return e;
   dv.beta = (const double*)gh.d_beta;
   dv.Kr = gh.d_Kr;
   dv.Hp = raman ? gh.d_Hp : nullptr;
-  dv.lor = gd.gain_on ? gh.d_lor : nullptr;
+  dv.lor = (gd.gain_on || yb) ? gh.d_lor : nullptr;
+  dv.lor2 = yb ? gh.d_lor2 : nullptr;
+  dv.ybw = yb ? (const double*)gh.d_ybw : nullptr;
   dv.nu = (const double*)gh.d_nu;
   dv.tw = gh.d_tw;
   dv.twl = gh.d_twl;
@@ -281,7 +301,7 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   dv.logm = gh.logm;
   dv.C = C;
   dv.raman = raman ? 1 : 0;
-  dv.gain = gd.gain_on ? 1 : 0;
+  dv.gain = yb ? 2 : (gd.gain_on ? 1 : 0);
   dv.alpha = gd.alpha;
   dv.fR = gd.f_R;
   dv.gain_log = gd.gain_log;
@@ -289,6 +309,11 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   dv.gain_len = gd.gain_length;
   dv.dt = gd.dt;
   dv.window_t = gd.window_t;
+  dv.yb_pp0 = yb ? gd.yb_pump_w : 0.0;
+  dv.yb_psat_p = yb ? gd.yb_pump_sat : 1.0;
+  dv.yb_ratio_p = yb ? gd.yb_pump_ratio : 0.0;
+  dv.yb_alpha_p = yb ? gd.yb_pump_alpha : 0.0;
+  dv.yb_eta_p = yb ? gd.yb_pump_eta : 0.0;
   return cudaSuccess;
 }
 
@@ -364,7 +389,9 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     const gnlse_grid_desc& gd = grids[i];
     const int n = gd.n;
     if (n < 256 || (n & (n - 1)) != 0 || !gd.beta_w || !(gd.dt > 0) || !(gd.window_t > 0) ||
-        (gd.gain_on && !(gd.E_sat > 0 && gd.gain_length > 0))) {
+        (gd.gain_on && !(gd.E_sat > 0 && gd.gain_length > 0)) ||
+        (gd.yb_on && (gd.gain_on || !gd.yb_alpha || !gd.yb_eta || !gd.yb_w_ratio || !gd.yb_w_sat ||
+                      !(gd.yb_pump_sat > 0) || !(gd.yb_pump_w >= 0)))) {
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
@@ -429,7 +456,8 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
-    if ((id.method == GNLSE_SS_SYM_RK4 || id.method == GNLSE_SS_SYMMETRIC) && grids[id.grid].gain_on) {
+    if ((id.method == GNLSE_SS_SYM_RK4 || id.method == GNLSE_SS_SYMMETRIC) &&
+        (grids[id.grid].gain_on || grids[id.grid].yb_on)) {
       free_plan(p);  // the split-step paths have no amplifier step
       return GNLSE_UNSUPPORTED;
     }
@@ -791,6 +819,7 @@ int gnlse_get_stats(gnlse_plan* p, gnlse_stats* out, void* stream) {
     o.ntraces = t.ntraces;
     o.trace_overflow = t.trace_overflow;
     o.finished = t.phase == 3 ? 1 : 0;
+    o.pump_w = t.pp;
   }
   return GNLSE_OK;
 }

@@ -608,13 +608,21 @@ struct Engine {
     const SV* Sf;
     const R* Kr;
     const R* lor;
-    R h, aA, ak0, a3, ao;
+    const R* lor2;
+    R h, aA, ak0, a3, ao, gb;
     double hh;
     int gain;
   };
 
+  // gain exponent of one linear-operator call: ga lor (saturable amplifier), or
+  // ga alpha_s N + gb eta_s (Yb model; ga = 500 h n2, gb = -500 h)
+  static __device__ __forceinline__ R gexp(const Op& op, int a, R ga) {
+    R x = ga * __ldg(&op.lor[a]);
+    if (op.gain == 2) x = fma(op.gb, __ldg(&op.lor2[a]), x);
+    return x;
+  }
   static __device__ __forceinline__ V mult(const Op& op, int a, V e, R ga) {
-    if (op.gain) e = cscale(e, (R)exp(ga * __ldg(&op.lor[a])));
+    if (op.gain) e = cscale(e, (R)exp(gexp(op, a, ga)));
     return e;
   }
   // complex64 value (or the leading part of a double-float value) of a state-like array
@@ -627,7 +635,7 @@ struct Engine {
   }
   // gain factor exp(ga * lor) as a double-float real, 1 + expm1(x)
   static __device__ __forceinline__ dff gain_df(const Op& op, int a, R ga) {
-    return fast_two_sum(1.0f, expm1f(ga * __ldg(&op.lor[a])));
+    return fast_two_sum(1.0f, expm1f(gexp(op, a, ga)));
   }
   static __device__ __forceinline__ dfc mult_df(const Op& op, int a, dfc e, R ga) {
     if (op.gain) e = dfc_scale(e, gain_df(op, a, ga));
@@ -828,6 +836,43 @@ struct Engine {
 
   static __device__ __forceinline__ R gain_a(const GridDev& g, double hh, double energy) {
     return (R)(g.gain_log * hh / (2.0 * g.gain_len) / (1.0 + energy / g.E_sat));
+  }
+
+  // Yb two-level model (Amplifier2LevelModel.factor, amplifier.py:346-379) for one
+  // linear-operator call over the step hh whose argument has inversion sums (sr, ss):
+  // the inversion n2 = N2 / N, the pump update Pp <- Pp exp(1000 hh g_p), and the
+  // coefficient 500 hh n2 of alpha_s N in the gain exponent (thread 0).
+  static __device__ __forceinline__ R yb_call(const GridDev& g, InstState& st, double hh, double sr,
+                                              double ss) {
+    const double tp = st.pp / g.yb_psat_p;
+    const double n2 = (g.yb_ratio_p * tp + sr) / (1.0 + tp + ss);
+    st.pp *= exp((g.yb_alpha_p * n2 - g.yb_eta_p) * hh * 1e3);
+    return (R)(500.0 * hh * n2);
+  }
+
+  // Yb model inversion sums sum_k w_ratio |X_k|^2, sum_k w_sat |X_k|^2 of a spectrum
+  // X = n fft(x) held in src (0: op.MA0, 1: op.acc, 2: the X buffer), over the cluster,
+  // into out[0..1] (shared memory; written by thread 0 before the closing barrier)
+  static __device__ __noinline__ void yb_sums(const Ctx& cx, const GridDev& g, const Op& op, int src,
+                                              double* out) {
+    const double2* w = (const double2*)g.ybw;
+    const int base = cx.rank * M;
+    double s0 = 0.0, s1 = 0.0;
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const V v = src == 0 ? op.MA0[a] : (src == 1 ? ldv(op.acc, a) : cx.X[pad(l)]);
+      const double p = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+      const double2 ww = __ldg(&w[a]);
+      s0 += ww.x * p;
+      s1 += ww.y * p;
+    }
+    double s[2] = {s0, s1};
+    cluster_sum<2>(cx, s);
+    if (threadIdx.x == 0) {
+      out[0] = s[0];
+      out[1] = s[1];
+    }
+    __syncthreads();
   }
 
   // ---- elementwise stage loops (fused end of one stage / start of the next) --
@@ -1163,6 +1208,8 @@ struct Engine {
     InstState st;
     Op op;
     double eA[2], eN[2];
+    double yA[2][2], yN[2][2];  // Yb model: inversion sums of the states and their N(A)
+    double yT[2][2];            // Yb model: sums of the third and fourth linear-call arguments
   };
   static_assert(sizeof(Ctl) <= 1024, "control block size");
 
@@ -1237,6 +1284,11 @@ struct Engine {
       c.eA[0] = c.st.cache_eA;
       c.eN[0] = c.st.cache_eN;
       c.eA[1] = c.eN[1] = 0.0;
+      c.yA[0][0] = c.st.cache_y[0];
+      c.yA[0][1] = c.st.cache_y[1];
+      c.yN[0][0] = c.st.cache_y[2];
+      c.yN[0][1] = c.st.cache_y[3];
+      c.yA[1][0] = c.yA[1][1] = c.yN[1][0] = c.yN[1][1] = 0.0;
     }
     __syncthreads();
     const GridDev& g = c.g;
@@ -1280,6 +1332,7 @@ struct Engine {
         st.z_ignore = d.length / d.traces;
         st.ma_valid = 0;
         st.ta = 0;
+        st.pp = g.yb_pp0;
         st.status = ST_RUNNING;
         st.phase = 1;
       }
@@ -1348,6 +1401,7 @@ struct Engine {
             const int m = e == 1 ? 1 : 0;
             op.Kr = (const R*)g.Kr;
             op.lor = (const R*)g.lor;
+            op.lor2 = (const R*)g.lor2;
             op.gain = g.gain;
             op.acc = base + 5 * N;
             op.Sf = base + 2 * N;
@@ -1357,17 +1411,24 @@ struct Engine {
             op.out = e == 1 ? base + 2 * N : Sh;
             op.h = (R)he;
             op.hh = 0.5 * he;
-            op.aA = g.gain ? gain_a(g, 0.5 * he, c.eA[m]) : (R)0;
-            op.ak0 = g.gain ? gain_a(g, 0.5 * he, he * he * c.eN[m]) : (R)0;
+            if (g.gain == 2) {  // linear calls 1 (S_I = L(A)) and 2 (k0 = L(h N(A)))
+              op.aA = yb_call(g, st, 0.5 * he, c.yA[m][0], c.yA[m][1]);
+              op.ak0 = yb_call(g, st, 0.5 * he, he * he * c.yN[m][0], he * he * c.yN[m][1]);
+              op.gb = (R)(-250.0 * he);
+            } else {
+              op.aA = g.gain ? gain_a(g, 0.5 * he, c.eA[m]) : (R)0;
+              op.ak0 = g.gain ? gain_a(g, 0.5 * he, he * he * c.eN[m]) : (R)0;
+            }
             op.a3 = op.ao = (R)0;
           }
           __syncthreads();
           pre_stage1(cx, op);
         } else if (kind == 0) {
           load_state(cx, mi == 0 ? S : Sh);
+          if (g.gain == 2) yb_sums(cx, g, op, 2, c.yA[mi]);
         }
         PROF_ADD(1);
-        const double en = nonlinear(cx, g, kind == 0 && g.gain);
+        const double en = nonlinear(cx, g, kind == 0 && g.gain == 1);
         PROF_ADD(0);
         if (kind == 0) {
           V* MA = reinterpret_cast<V*>(base + (3 + mi) * N);
@@ -1376,7 +1437,11 @@ struct Engine {
           if (g.gain) {
             if (threadIdx.x == 0) op.MA0 = MA;
             __syncthreads();
-            eN = energy_of(cx, g, op, 0);
+            if (g.gain == 2) {
+              yb_sums(cx, g, op, 0, c.yN[mi]);
+            } else {
+              eN = energy_of(cx, g, op, 0);
+            }
           }
           if (threadIdx.x == 0) {
             c.eA[mi] = en;
@@ -1385,6 +1450,10 @@ struct Engine {
               st.ma_valid = 1;
               st.cache_eA = en;
               st.cache_eN = eN;
+              st.cache_y[0] = c.yA[0][0];
+              st.cache_y[1] = c.yA[0][1];
+              st.cache_y[2] = c.yN[0][0];
+              st.cache_y[3] = c.yN[0][1];
             }
           }
           __syncthreads();
@@ -1392,7 +1461,16 @@ struct Engine {
           post_stage1(cx, op);
         } else if (kind == 2) {
           post_stage2(cx, op);
-          if (g.gain) {
+          if (g.gain == 2) {
+            yb_sums(cx, g, op, 2, c.yT[0]);
+            yb_sums(cx, g, op, 1, c.yT[1]);
+            if (threadIdx.x == 0) {  // linear call 3 (L(S_I + k2)), then call 4 (L(acc))
+              op.a3 = yb_call(g, st, op.hh, c.yT[0][0], c.yT[0][1]);
+              op.ao = yb_call(g, st, op.hh, c.yT[1][0], c.yT[1][1]);
+            }
+            __syncthreads();
+            scale_stage3(cx, op);
+          } else if (g.gain) {
             const double e_acc = energy_of(cx, g, op, 1);
             const double e_u = energy_of(cx, g, op, 2);
             if (threadIdx.x == 0) {

@@ -102,6 +102,7 @@ extern "C" int gnlse_propagate_noalloc(const gnlse_grid_desc* gd, const gnlse_in
   const int n = gd->n;
   if (n < 256 || n > kNoAllocMaxN || (n & (n - 1)) != 0) return GNLSE_UNSUPPORTED;
   if (gd->cluster > 1 || !gd->beta_w || !(gd->dt > 0) || !(gd->window_t > 0)) return GNLSE_BAD_ARGUMENT;
+  if (gd->yb_on) return GNLSE_UNSUPPORTED;  // the Yb model's tables have no room in the static array
   if ((id->method != GNLSE_RK4IP && id->method != GNLSE_ARK4IP) || id->total_steps < 1 ||
       id->traces < 1 || id->max_traces != 0 || !(id->length >= 0) ||
       (id->method == GNLSE_ARK4IP && !(id->local_error > 0)) ||

@@ -13,7 +13,9 @@ struct GridDev {
   const double* beta;   // [N] sum_n beta_n (w-w0)^n/n!   (1/km), FP64
   const void* Kr;       // [N] real: gamma * (1 + omega * s)
   const void* Hp;       // [N] complex: fft(h_R) * window_t / N   (null: no Raman)
-  const void* lor;      // [N] real: gain profile                   (null: no gain)
+  const void* lor;      // [N] real: gain profile (Yb model: alpha_s N, 1/m) (null: no gain)
+  const void* lor2;     // [N] real: Yb model eta_s (1/m)            (null: not the Yb model)
+  const double* ybw;    // [2N] FP64: Yb model inversion weights (w_ratio, w_sat) per entry
   const double* nu;     // [N] absolute frequency (THz), FP64, for photon number
   const void* tw;       // [N] natural order: exp(+2 pi i j / N) (cross-CTA pass)
   const void* twl;      // [M] natural order: exp(+2 pi i j / M) (per-CTA transform)
@@ -23,7 +25,7 @@ struct GridDev {
   const void* twp64;    // extended-state plans: FP64 copy of twp
   const void* cis_df;   // extended-state plans: [1024] double-float cis(j pi / 512)
   int n, logm, C, raman;
-  int gain, pad0;
+  int gain, pad0;       // gain 1: saturable amplifier, 2: Yb two-level model
   double alpha;         // 1/km, linear attenuation
   double fR;            // Raman fraction
   double gain_log;      // ln(10^(gain_dB/10))
@@ -31,6 +33,7 @@ struct GridDev {
   double gain_len;      // km (amplifier length = fibre length)
   double dt;            // ps
   double window_t;      // ps
+  double yb_pp0, yb_psat_p, yb_ratio_p, yb_alpha_p, yb_eta_p;  // Yb pump (W, W, -, 1/m, 1/m)
 };
 
 struct InstDev {
@@ -58,6 +61,8 @@ struct InstState {
   double z, h, z_ignore, delta_last;
   double E_in, E_out, Nph_in, Nph_out;
   double cache_eA, cache_eN;  // gain energies of the cached state
+  double cache_y[4];          // Yb model: inversion sums of the cached state and its N(A)
+  double pp;                  // Yb model: pump power, W
   long long attempts, accepted, rejected, evals, steps, ffts;
   int status, ntraces, phase, sidx;
   int ma_valid, ta, trace_overflow, pad0;

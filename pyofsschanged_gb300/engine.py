@@ -82,6 +82,13 @@ class Plan:
             d.E_sat = g.E_sat
             d.gain_length = g.gain_length
             d.gain_profile = _ptr(g.gain_profile)
+            yb = g.yb
+            if yb is not None:
+                d.yb_on = 1
+                d.yb_pump_w, d.yb_pump_sat, d.yb_pump_ratio = yb.Pp_0, yb.Psat_p, yb.ratio_p
+                d.yb_pump_alpha, d.yb_pump_eta = yb.alpha_p_N, yb.eta_p
+                d.yb_alpha, d.yb_eta = _ptr(yb.alpha_s_N), _ptr(yb.eta_s)
+                d.yb_w_ratio, d.yb_w_sat = _ptr(yb.w_ratio), _ptr(yb.w_sat)
         idesc = (nat.InstanceDesc * len(self.instances))()
         for i, s in enumerate(self.instances):
             d = idesc[i]

@@ -12,8 +12,11 @@ transforms with a double-float propagation state), ``"fp32"`` (complex64
 throughout) or ``"fp64"`` (complex128 throughout).  The stepper exceptions of
 pyofss/modules/stepper.py:33-47 are raised with the same names.
 
-Models outside the CUDA path (WDM two-channel, the legacy ``raman_scattering``
-rs_factor terms, Er/Yb gain models, ASE noise) raise ``NotImplementedError``.
+The saturable amplifier and the Yb two-level gain (``use_Yb_model``; its cross
+sections from ``yb_cross_sections`` or an importable pyofss installation, its pump
+power after the run in ``fibre.amplifier.Pp``) run with the RK4IP methods.  Models
+outside the CUDA path (WDM two-channel, the legacy ``raman_scattering`` rs_factor
+terms, the Er gain profile, ASE noise) raise ``NotImplementedError``.
 """
 
 import numpy as np
@@ -114,7 +117,7 @@ class Fibre:
                  small_signal_gain=None, E_sat=None, P_sat=None, Tr=None, lamb0=None,
                  bandwidth=None, use_Er_profile=False, use_Er_noise=False, use_Yb_model=False,
                  Pp_0=None, N=None, Rr=None, dir=None, save_represent="power", cycle=None,
-                 downsampling=None, precision="mixed", cluster=0):
+                 downsampling=None, precision="mixed", cluster=0, yb_cross_sections=None):
         m = method.lower()
         if m.startswith("cuda_"):
             m = m[5:]
@@ -125,8 +128,10 @@ class Fibre:
             raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
         if raman_scattering and not use_all:
             raise NotImplementedError("legacy rs_factor Raman model is not on the CUDA path")
-        if use_Er_profile or use_Er_noise or use_Yb_model:
-            raise NotImplementedError("Er/Yb gain models and ASE noise are not on the CUDA path")
+        if use_Er_profile or use_Er_noise:
+            raise NotImplementedError("the Er gain profile and ASE noise are not on the CUDA path")
+        if use_Yb_model and m in ("ss_sym_rk4", "ss_symmetric"):
+            raise NotImplementedError("the split-step methods run without gain on the CUDA path")
         if small_signal_gain is not None and E_sat is None and P_sat is not None:
             if Tr is None:
                 raise Exception("Repetition rate is not defined.")
@@ -139,6 +144,9 @@ class Fibre:
         self.centre_omega = centre_omega
         self.small_signal_gain, self.E_sat = small_signal_gain, E_sat
         self.lamb0, self.bandwidth = lamb0, bandwidth
+        self.use_Yb_model, self.Pp_0, self.N, self.Rr = use_Yb_model, Pp_0, N, Rr
+        self.yb_cross_sections = yb_cross_sections
+        self.amplifier = None
         self.method = m
         self.precision = precision
         self.cluster = cluster
@@ -153,7 +161,10 @@ class Fibre:
                        tau_1=self.tau_1, tau_2=self.tau_2, f_R=self.f_R,
                        centre_omega=self.centre_omega, small_signal_gain=self.small_signal_gain,
                        E_sat=self.E_sat, length=self.length, lamb0=self.lamb0,
-                       bandwidth=self.bandwidth, cluster=self.cluster)
+                       bandwidth=self.bandwidth, use_Yb_model=self.use_Yb_model, Pp_0=self.Pp_0,
+                       N=self.N, Rr=self.Rr, yb_cross_sections=self.yb_cross_sections,
+                       cluster=self.cluster)
+        self.amplifier = g.yb
         st = self.stepper
         inst = Instance(0, method=st.method, length=self.length, local_error=st.local_error,
                         total_steps=st.total_steps, traces=st.traces)
@@ -171,6 +182,8 @@ class Fibre:
         torch.cuda.current_stream(plan.device).synchronize()
         st = stats[0]
         self.stepper.stats = st
+        if self.amplifier is not None:  # Amplifier2LevelModel.Pp after update_Pp calls
+            self.amplifier.Pp = st["pump_w"]
         storage = self.stepper.storage
         storage.reset_array()
         storage.reset_characts()

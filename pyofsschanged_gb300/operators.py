@@ -10,10 +10,14 @@ These are the tables pyofss builds once per domain:
   (nonlinearity.py:72-100) model (``Nonlinearity.__call__``, nonlinearity.py:160-185);
 * saturable gain: ``ln(10^(gain_dB/10))``, ``E_sat``, the fibre length and the
   Lorentzian profile ``1 / (1 + 4 (nu - nu0)^2 / dnu^2)`` with
-  ``dnu = c bandwidth / lamb0^2`` in FFT order (``Amplifier``, amplifier.py:57-158).
+  ``dnu = c bandwidth / lamb0^2`` in FFT order (``Amplifier``, amplifier.py:57-158);
+* the Yb two-level gain (``Amplifier2LevelModel``, amplifier.py:178-379): the
+  per-frequency gain and inversion tables and the pump constants.
 """
 
+import importlib.util
 import math
+import os
 
 import numpy as np
 from scipy.integrate import simpson
@@ -98,12 +102,119 @@ def gain_profile(domain, lamb0=None, bandwidth=None):
     return fftshift(prof)
 
 
+def read_cross_section_table(path):
+    """(wavelength m, sigma_12 m^2, sigma_21 m^2) columns of a Yb cross-section table
+    such as pyofss/data/CrossSectionDataExp.txt.  As ``Amplifier2LevelModel`` reads it
+    (pandas ``read_csv`` with its default header inference, amplifier.py:238-242), the
+    first line names the columns and is not data."""
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    tab = np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]])
+    return tab[:, 0], tab[:, 1], tab[:, 2]
+
+
+def _reference_cross_section_file():
+    spec = importlib.util.find_spec("pyofss")
+    if spec is None or not spec.submodule_search_locations:
+        return None
+    for root in spec.submodule_search_locations:
+        path = os.path.join(root, "data", "CrossSectionDataExp.txt")
+        if os.path.exists(path):
+            return path
+    return None
+
+
+class Amplifier2LevelModel:
+    """Yb two-level rate-equation gain (pyofss/modules/amplifier.py:178-379).
+
+    ``Pp`` (W), ``N`` (Yb density, 1e25 m^-3) and ``Rr`` (repetition rate, THz) as in
+    the reference.  ``cross_sections`` gives the signal cross sections: a path to a
+    table in the reference's format, ``(wavelength_m, sigma_12, sigma_21)`` columns, or
+    ``(sigma_12, sigma_21)`` already on the domain (natural order, m^2).  By default the
+    table of an importable pyofss installation is used.  The engine evaluates
+    ``factor`` (amplifier.py:366-379) on the GPU; ``Pp`` holds the pump power reached
+    by the last propagation.
+    """
+
+    h_p = 6.62e-34          # amplifier.py:201-218
+    T = 850.0e-6
+    a = 3.0e-6
+    b = 60.0e-6
+    NA = 0.13
+    lamb_p = 976.0
+    sigma12_p = 2.5e-24
+    sigma21_p = 2.44e-24
+
+    def __init__(self, name="amplifier2LevelModel", Pp=None, N=None, Rr=None, cross_sections=None):
+        if Pp is None or N is None or Rr is None:
+            raise ValueError("Amplifier2LevelModel needs Pp, N and Rr")
+        self.name = name
+        self.Pp_0 = float(Pp)
+        self.Pp = self.Pp_0
+        self.N = N * 1e25 * np.pi * self.a ** 2
+        self.Tr = 1.0 / Rr
+        self.cross_sections = cross_sections
+        self.domain = None
+
+    def _sigma_s(self, domain):
+        cs = self.cross_sections
+        if cs is None:
+            cs = _reference_cross_section_file()
+            if cs is None:
+                raise FileNotFoundError(
+                    "Amplifier2LevelModel needs the Yb cross sections: pass cross_sections= "
+                    "(a table path, (wavelength_m, sigma_12, sigma_21) or (sigma_12, sigma_21) on the domain)")
+        if isinstance(cs, (str, os.PathLike)):
+            cs = read_cross_section_table(cs)
+        if len(cs) == 2:
+            s12, s21 = (np.asarray(x, float) for x in cs)
+            if s12.shape != (domain.total_samples,) or s21.shape != s12.shape:
+                raise ValueError("on-grid cross sections must have one value per sample")
+            return s12, s21
+        from scipy.interpolate import InterpolatedUnivariateSpline as IUS
+        lam, c12, c21 = (np.asarray(x, float) for x in cs)
+        s12 = IUS(lam * 1e9, c12 * 1e27, ext=1)(domain.Lambda) * 1e-27
+        s21 = IUS(lam * 1e9, c21 * 1e27, ext=1)(domain.Lambda) * 1e-27
+        return s12, s21
+
+    def set_domain(self, domain):
+        """Tables on ``domain`` (amplifier.py:247-344), in the engine's form: FFT order,
+        signal gain alpha_s N and eta_s (1/m), and the inversion weights that turn
+        |n fft(x)|^2 into Ps / Psat_s terms (Ps = spectral power * n dt / Tr)."""
+        a = self.a
+        s12, s21 = self._sigma_s(domain)
+        self.sigma12_s, self.sigma21_s = s12, s21
+        V = (2.0 * np.pi / domain.Lambda) * a * self.NA * 1e9
+        omega_s = a * (0.616 + 1.66 / pow(V, 1.5) + 0.987 / pow(V, 6.0))
+        rho_s = (1.0 - np.exp(-2.0 * a ** 2 / (omega_s * omega_s))) / (np.pi * a ** 2)
+        rho_p = (a ** 2) / (self.b ** 2) / (np.pi * a ** 2)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            psat_s = (self.h_p * domain.nu * 1e12) / (self.T * (s12 + s21) * rho_s)
+            ratio_s = s12 / (s12 + s21)
+            w_ratio = ratio_s / psat_s
+            w_sat = 1.0 / psat_s
+        scale = domain.dt / (domain.total_samples * self.Tr)
+        # terms the reference drops as NaN (zero cross sections) weigh nothing
+        self.w_ratio = np.ascontiguousarray(fftshift(np.nan_to_num(w_ratio, nan=0.0) * scale), float)
+        self.w_sat = np.ascontiguousarray(fftshift(np.nan_to_num(w_sat, nan=0.0) * scale), float)
+        self.alpha_s_N = np.ascontiguousarray(fftshift((s12 + s21) * rho_s * self.N), float)
+        self.eta_s = np.ascontiguousarray(fftshift(s12 * rho_s * self.N), float)
+        sp = self.sigma12_p + self.sigma21_p
+        self.Psat_p = (self.h_p * lambda_to_nu(self.lamb_p) * 1e12) / (self.T * sp * rho_p)
+        self.ratio_p = self.sigma12_p / sp
+        self.alpha_p_N = sp * rho_p * self.N
+        self.eta_p = self.sigma12_p * rho_p * self.N
+        self.domain = domain
+        return self
+
+
 class GridTables:
     """All per-grid arrays and scalars of one (domain, fibre model) pair."""
 
     def __init__(self, domain, beta=None, alpha=None, gamma=0.0, self_steepening=False,
                  use_all=False, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18, centre_omega=None,
                  small_signal_gain=None, E_sat=None, length=1.0, lamb0=None, bandwidth=None,
+                 use_Yb_model=False, Pp_0=None, N=None, Rr=None, yb_cross_sections=None,
                  cluster=0):
         self.domain = domain
         self.n = domain.total_samples
@@ -120,7 +231,10 @@ class GridTables:
         self.hR_re = None if hr is None else np.ascontiguousarray(hr.real, float)
         self.hR_im = None if hr is None else np.ascontiguousarray(hr.imag, float)
         self.nu = np.ascontiguousarray(fftshift(domain.nu), float)
-        self.gain_on = small_signal_gain is not None and E_sat is not None
+        # fibre.py:97-103: the Yb model replaces the saturable amplifier
+        self.yb = (Amplifier2LevelModel(Pp=Pp_0, N=N, Rr=Rr, cross_sections=yb_cross_sections)
+                   .set_domain(domain) if use_Yb_model else None)
+        self.gain_on = small_signal_gain is not None and E_sat is not None and not use_Yb_model
         self.gain_log = math.log(math.pow(10.0, 0.1 * small_signal_gain)) if self.gain_on else 0.0
         self.E_sat = float(E_sat) if self.gain_on else 0.0
         self.gain_length = float(length)

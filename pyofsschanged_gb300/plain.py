@@ -33,6 +33,8 @@ class PlainRK4IP:
             self.hR = torch.complex(torch.as_tensor(g.hR_re, device=self.dev),
                                     torch.as_tensor(g.hR_im, device=self.dev)).to(dtype)
             self.fR = g.f_R
+        if getattr(g, "yb", None) is not None:
+            raise NotImplementedError("the plain comparison path has no Yb gain model")
         self.gain = g.gain_on
         if self.gain:
             self.gain_log, self.E_sat, self.glen = g.gain_log, g.E_sat, g.gain_length

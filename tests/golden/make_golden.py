@@ -116,6 +116,21 @@ CASES = {
         fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
                    use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
                    method="ss_symmetric", total_steps=800, traces=1)),
+    # Yb two-level gain (Amplifier2LevelModel, amplifier.py:178-344): 1 ps Gaussian at
+    # 1030 nm through a pumped Yb fibre; the fixture also keeps the reference's cross
+    # sections interpolated on the grid and its pump power after the propagation.
+    "yb_ark4ip_1024": dict(
+        domain=dict(bit_width=100.0, samples_per_bit=1024, lambda_nm=1030.0),
+        pulse=dict(kind="gaussian", peak_power=100.0, width=1.0, using_fwhm=True),
+        fibre=dict(length=5.0e-4, beta=[0.0, 0.0, 25.0, 0.05], gamma=5.0,
+                   self_steepening=True, use_all="blowwood", use_Yb_model=True, Pp_0=2.0,
+                   N=2.0, Rr=1.0e-5, method="ark4ip", local_error=1e-6, traces=1)),
+    "yb_fixed_2048": dict(
+        domain=dict(bit_width=100.0, samples_per_bit=2048, lambda_nm=1030.0),
+        pulse=dict(kind="gaussian", peak_power=100.0, width=1.0, using_fwhm=True, C=-3.0),
+        fibre=dict(length=3.0e-4, beta=[0.0, 0.0, 25.0, 0.05], gamma=5.0,
+                   use_Yb_model=True, Pp_0=5.0, N=5.0, Rr=1.0e-5, method="rk4ip",
+                   total_steps=200, traces=4)),
 }
 
 SLOW = {"sc_cfg_8192"}
@@ -155,6 +170,10 @@ def run_case(name, spec):
     out = dict(A0=A0, A_out=A_out, rk4ip_calls=calls, step_sizes=steps, trace_z=trace_z,
                trace_peak=trace_peak, fft_total=np.int64(st.fft_total),
                wall_s=np.float64(wall), params=np.array(json.dumps(params)))
+    if spec["fibre"].get("use_Yb_model"):
+        amp = fib.amplifier
+        out.update(yb_pump_out=np.float64(amp.Pp), yb_sigma12_s=np.asarray(amp.sigma12_s, float),
+                   yb_sigma21_s=np.asarray(amp.sigma21_s, float))
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(f"{name}: {wall:.2f} s, {len(calls)} rk4ip calls, fft {st.fft_total}, "
           f"peak_out {np.max(np.abs(A_out) ** 2):.6g}", flush=True)

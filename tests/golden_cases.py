@@ -16,6 +16,8 @@ def load(name):
     case = {k: z[k] for k in z.files if k != "params"}
     case["params"] = json.loads(str(z["params"]))
     case["name"] = name
+    if "yb_sigma12_s" in case:  # the reference's cross sections interpolated on the grid
+        case["params"]["fibre"]["yb_cross_sections"] = (case["yb_sigma12_s"], case["yb_sigma21_s"])
     return case
 
 

@@ -37,6 +37,25 @@ def test_system_with_cuda_fibre(cuda_ready, name, precision, tol):
     np.testing.assert_allclose(st.storage.z, case["trace_z"], rtol=1e-9 if precision == "fp64" else 2e-3)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-4)])
+def test_yb_fibre_in_system(cuda_ready, precision, tol):
+    """Fibre(use_Yb_model=True) in a System: output and pump power as the reference's."""
+    case = gc.load("yb_ark4ip_1024")
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    p = dict(prm["pulse"])
+    p.pop("kind")
+    fk = gc.fibre_kwargs(prm)
+    fk["method"] = "cuda_" + fk["method"]
+    sys_ = System(d)
+    sys_.add(Gaussian(**p))
+    sys_.add(Fibre(precision=precision, **fk))
+    sys_.run()
+    assert spec_err(sys_.fields["fibre"], case["A_out"]) <= tol
+    assert sys_["fibre"].amplifier.Pp == pytest.approx(float(case["yb_pump_out"]),
+                                                      rel=1e-9 if precision == "fp64" else 1e-5)
+
+
 def test_fibre_raises_reference_exception(cuda_ready):
     d = Domain(bit_width=12.5, samples_per_bit=1024, centre_nu=359.0)
     a = Sech(peak_power=100.0, width=0.1)(d, np.zeros(1024, complex))

@@ -102,7 +102,8 @@ def test_fp32_matches_reference(cuda_ready, name):
     ("sc_blowwood_fixed_4096", "mixed", 1), ("ss_sym_rk4_sc_1024", "fp64", 2),
     ("ss_sym_rk4_sc_1024", "mixed", 4), ("ss_sym_rk4_soliton_1024", "fp32", 2),
     ("ss_symmetric_sc_1024", "fp64", 2), ("ss_symmetric_sc_1024", "mixed", 4),
-    ("ss_symmetric_soliton_1024", "fp32", 2)])
+    ("ss_symmetric_soliton_1024", "fp32", 2), ("yb_ark4ip_1024", "fp64", 2),
+    ("yb_ark4ip_1024", "mixed", 4), ("yb_fixed_2048", "fp64", 4), ("yb_fixed_2048", "mixed", 2)])
 def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     case = gc.load(name)
     _, out, st = run(case, precision, cluster)
@@ -115,6 +116,18 @@ def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     else:
         assert spec_err(out, case["A_out"]) <= (FP32_SPLIT_STEP_TOL if name.startswith("ss_")
                                                  else FP32_SPEC_TOL)
+
+
+@pytest.mark.parametrize("name", ["yb_ark4ip_1024", "yb_fixed_2048"])
+@pytest.mark.parametrize("precision,cluster", [("fp64", 0), ("mixed", 0), ("fp64", 2)])
+def test_yb_pump_power_matches_reference(cuda_ready, name, precision, cluster):
+    """Amplifier2LevelModel.update_Pp runs on every linear-operator call, rejected
+    attempts included (amplifier.py:360-379): the pump power the engine reaches
+    equals the reference's."""
+    case = gc.load(name)
+    _, _, st = run(case, precision, cluster)
+    want = float(case["yb_pump_out"])
+    assert st["pump_w"] == pytest.approx(want, rel=1e-9 if precision == "fp64" else 1e-5)
 
 
 def test_fixed_step_traces(cuda_ready):

@@ -105,4 +105,56 @@ def test_abi_library_exports_every_declared_symbol():
         assert hasattr(lib, s), s
     assert set(syms) == set(_native.SIGNATURES)
     lib.gnlse_abi_version.restype = ct.c_int
-    assert lib.gnlse_abi_version() == 1
+    assert lib.gnlse_abi_version() == 2
+
+
+@pytest.mark.parametrize("name", ["yb_ark4ip_1024", "yb_fixed_2048"])
+def test_yb_tables_match_oracle(name):
+    """Amplifier2LevelModel tables (amplifier.py:247-344) in the engine's form against
+    the oracle's restatement: gain exponent and inversion weights per frequency."""
+    case = gc.load(name)
+    prm = case["params"]
+    fk = gc.fibre_kwargs(prm)
+    d = Domain(**gc.domain_kwargs(prm))
+    g = GridTables(d, beta=fk["beta"], gamma=fk["gamma"], use_Yb_model=True, Pp_0=fk["Pp_0"],
+                   N=fk["N"], Rr=fk["Rr"], yb_cross_sections=fk["yb_cross_sections"])
+    grid = go.Grid(**gc.domain_kwargs(prm))
+    o = go.YbGain(grid, fk["Pp_0"], fk["N"], fk["Rr"], *fk["yb_cross_sections"])
+    yb = g.yb
+    assert not g.gain_on
+    np.testing.assert_allclose(yb.alpha_s_N, go.fftshift(o.alpha_s * o.N), rtol=1e-14)
+    np.testing.assert_allclose(yb.eta_s, go.fftshift(o.eta_s), rtol=1e-14)
+    assert yb.Psat_p == pytest.approx(o.Psat_p, rel=1e-15)
+    assert yb.ratio_p == o.ratio_p
+    assert yb.alpha_p_N == pytest.approx(o.alpha_p * o.N, rel=1e-15)
+    assert yb.eta_p == pytest.approx(o.eta_p, rel=1e-15)
+    # the inversion sums of a field equal the oracle's sums over Ps / Psat_s
+    rng = np.random.default_rng(3)
+    a = case["A0"] * (1.0 + 0.1 * rng.standard_normal(d.total_samples))
+    X = d.total_samples * go.fft(a)  # the engine's spectral scale, FFT order
+    Ps = go.spectral_power(a) * len(a) * grid.dt / o.Tr
+    with np.errstate(divide="ignore", invalid="ignore"):
+        x, y = o.ratio_s * Ps / o.Psat_s, Ps / o.Psat_s
+    assert np.sum(yb.w_ratio * np.abs(X) ** 2) == pytest.approx(np.sum(x[~np.isnan(x)]), rel=1e-12)
+    assert np.sum(yb.w_sat * np.abs(X) ** 2) == pytest.approx(np.sum(y[~np.isnan(y)]), rel=1e-12)
+
+
+def test_yb_cross_section_table_reading(tmp_path):
+    """The reference reads its table with a header line; values interpolate with
+    zero outside the table."""
+    lam = np.linspace(1000e-9, 1060e-9, 61)
+    s12 = 1e-25 * np.exp(-((lam - 1030e-9) / 10e-9) ** 2)
+    s21 = 2e-25 * np.exp(-((lam - 1035e-9) / 12e-9) ** 2)
+    path = tmp_path / "cs.txt"
+    rows = [f"{a:.6E}, {b:.6E}, {c:.6E}" for a, b, c in zip(lam, s12, s21)]
+    path.write_text("\n".join(rows) + "\n")
+    from pyofsschanged_gb300.operators import Amplifier2LevelModel, read_cross_section_table
+    l2, a2, b2 = read_cross_section_table(str(path))
+    assert len(l2) == 60 and l2[0] == pytest.approx(lam[1], rel=1e-6)
+    d = Domain(bit_width=100.0, samples_per_bit=1024, centre_nu=299792.458 / 1030.0)
+    amp = Amplifier2LevelModel(Pp=1.0, N=1.0, Rr=1e-5, cross_sections=str(path)).set_domain(d)
+    grid = go.Grid(bit_width=100.0, samples_per_bit=1024, centre_nu=299792.458 / 1030.0)
+    o12, o21 = go.yb_cross_sections(grid, str(path))
+    np.testing.assert_allclose(amp.sigma12_s, o12, rtol=1e-14, atol=0)
+    np.testing.assert_allclose(amp.sigma21_s, o21, rtol=1e-14, atol=0)
+    assert np.all(amp.sigma12_s[d.Lambda > 1060.0] == 0.0)

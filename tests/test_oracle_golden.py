@@ -101,3 +101,29 @@ def test_oracle_sc_cfg_8192():
     p, out, _ = run_oracle(case)
     assert rel_l2(out, case["A_out"]) <= 1e-10
     assert p.evals == gc.expected_evals(case)
+
+
+YB = [n for n in FAST if n.startswith("yb_")]
+
+
+@pytest.mark.parametrize("name", YB)
+def test_oracle_yb_pump_power(name):
+    """Amplifier2LevelModel advances the pump power on every linear-operator call
+    (amplifier.py:360-379); the oracle ends with the reference's pump power."""
+    case = gc.load(name)
+    p, _, _ = run_oracle(case)
+    assert p.gain.Pp == pytest.approx(float(case["yb_pump_out"]), rel=1e-12)
+
+
+@pytest.mark.parametrize("name", YB)
+def test_oracle_yb_cross_sections(name):
+    """interpolate_sigma_s (amplifier.py:234-245) restated on the reference's own table."""
+    from oracle import ref_shim
+    path = os.path.join(ref_shim.REFERENCE_ROOT, "pyofss", "data", "CrossSectionDataExp.txt")
+    if not os.path.exists(path):
+        pytest.skip("reference data table absent")
+    case = gc.load(name)
+    grid = go.Grid(**gc.domain_kwargs(case["params"]))
+    s12, s21 = go.yb_cross_sections(grid, path)
+    np.testing.assert_allclose(s12, case["yb_sigma12_s"], rtol=1e-13, atol=1e-40)
+    np.testing.assert_allclose(s21, case["yb_sigma21_s"], rtol=1e-13, atol=1e-40)

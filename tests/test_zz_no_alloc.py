@@ -86,3 +86,20 @@ def test_noalloc_rejects_large_grid(cuda_ready):
     rc = nat.lib().gnlse_propagate_noalloc(ct.byref(gd), ct.byref(idesc), ct.c_void_p(f.data_ptr()),
                                            None, ct.c_void_p(0))
     assert rc == nat.GNLSE_UNSUPPORTED
+
+
+def test_noalloc_rejects_yb_model(cuda_ready):
+    case = gc.load("yb_ark4ip_1024")
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    fk = gc.fibre_kwargs(prm)
+    for k in ("method", "total_steps", "traces", "local_error"):
+        fk.pop(k, None)
+    g = GridTables(d, **fk)
+    inst = Instance(0, method="ark4ip", length=fk["length"], local_error=1e-6, traces=1)
+    gd, idesc = descs(g, inst)
+    gd.yb_on = 1
+    f = torch.as_tensor(case["A0"].astype(np.complex64)).cuda()
+    rc = nat.lib().gnlse_propagate_noalloc(ct.byref(gd), ct.byref(idesc), ct.c_void_p(f.data_ptr()),
+                                           None, ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == nat.GNLSE_UNSUPPORTED
