@@ -285,9 +285,12 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   if (yb && (e = upload(p, ybw, &gh.d_ybw)) != cudaSuccess) return e;
   dv.beta = (const double*)gh.d_beta;
   dv.Kr = gh.d_Kr;
-  dv.Hp = raman ? gh.d_Hp : nullptr;
-  dv.lor = (gd.gain_on || yb) ? gh.d_lor : nullptr;
-  dv.lor2 = yb ? gh.d_lor2 : nullptr;
+  // Tables a grid does not use point at tables of the same type and length, never at
+  // null: the kernels read them only under their flags (raman, gain), but the compiler
+  // may issue such a read-only load ahead of its branch.
+  dv.Hp = raman ? gh.d_Hp : gh.d_tw;
+  dv.lor = (gd.gain_on || yb) ? gh.d_lor : gh.d_Kr;
+  dv.lor2 = yb ? gh.d_lor2 : gh.d_Kr;
   dv.ybw = yb ? (const double*)gh.d_ybw : nullptr;
   dv.nu = (const double*)gh.d_nu;
   dv.tw = gh.d_tw;

@@ -142,8 +142,11 @@ extern "C" int gnlse_propagate_noalloc(const gnlse_grid_desc* gd, const gnlse_in
   memset(&g, 0, sizeof(g));
   g.beta = (const double*)(base + kBeta);
   g.Kr = base + kKr;
-  g.Hp = raman ? base + kHp : nullptr;
-  g.lor = gain ? base + kLor : nullptr;
+  // unused tables still point at valid memory: a read-only load may be issued ahead
+  // of the flag that guards it
+  g.Hp = base + kHp;
+  g.lor = base + kLor;
+  g.lor2 = base + kLor;
   g.nu = (const double*)(base + kNu);
   g.tw = base + kTw;
   g.twl = base + kTw;

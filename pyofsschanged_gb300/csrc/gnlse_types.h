@@ -12,9 +12,11 @@ namespace gnlse {
 struct GridDev {
   const double* beta;   // [N] sum_n beta_n (w-w0)^n/n!   (1/km), FP64
   const void* Kr;       // [N] real: gamma * (1 + omega * s)
-  const void* Hp;       // [N] complex: fft(h_R) * window_t / N   (null: no Raman)
-  const void* lor;      // [N] real: gain profile (Yb model: alpha_s N, 1/m) (null: no gain)
-  const void* lor2;     // [N] real: Yb model eta_s (1/m)            (null: not the Yb model)
+  // Hp, lor and lor2 of a grid without Raman / gain / the Yb model point at another
+  // table of the same type and length (read only under the raman and gain flags)
+  const void* Hp;       // [N] complex: fft(h_R) * window_t / N
+  const void* lor;      // [N] real: gain profile (Yb model: alpha_s N, 1/m)
+  const void* lor2;     // [N] real: Yb model eta_s (1/m)
   const double* ybw;    // [2N] FP64: Yb model inversion weights (w_ratio, w_sat) per entry
   const double* nu;     // [N] absolute frequency (THz), FP64, for photon number
   const void* tw;       // [N] natural order: exp(+2 pi i j / N) (cross-CTA pass)
