@@ -40,6 +40,11 @@
 #ifndef GNLSE_PPT
 #define GNLSE_PPT 16
 #endif
+// fewest threads per CTA (slices below GNLSE_PPT * this many points leave threads
+// idle in the radix passes)
+#ifndef GNLSE_TMIN
+#define GNLSE_TMIN 64
+#endif
 
 namespace cg = cooperative_groups;
 
@@ -176,7 +181,7 @@ struct Engine {
   static_assert(!XS || sizeof(R) == 4, "extended state runs on complex64 transforms");
   static constexpr int M = 1 << LOGM;
   static constexpr int N = M * C;
-  static constexpr int T = (M / GNLSE_PPT) < 64 ? 64 : (M / GNLSE_PPT);
+  static constexpr int T = (M / GNLSE_PPT) < GNLSE_TMIN ? GNLSE_TMIN : (M / GNLSE_PPT);
   static constexpr int MP = M + M / 16;
   static constexpr int RB = GNLSE_RADIX_BITS;  // log2 of the main radix (gnlse_twiddle.h)
   static constexpr int RADIX = 1 << RB;

@@ -96,15 +96,15 @@ def test_fp32_matches_reference(cuda_ready, name):
 @pytest.mark.parametrize("name,precision,cluster", [
     ("sc_blowwood_ark4ip_1024", "fp64", 2), ("sc_blowwood_ark4ip_1024", "fp64", 4),
     ("gain_ark4ip_1024", "fp64", 2), ("sc_hollenbeck_ark4ip_2048", "fp64", 2),
-    ("soliton_n2_1024", "fp32", 2), ("soliton_n2_1024", "fp32", 4),
+    ("soliton_test_solver_2048", "fp32", 2), ("spm_loss_fixed_2048", "fp32", 2),
     ("spm_loss_fixed_2048", "fp64", 2), ("sc_blowwood_fixed_4096", "fp64", 2),
     ("sc_blowwood_fixed_4096", "fp32", 1), ("soliton_test_solver_2048", "fp32", 1),
     ("sc_blowwood_ark4ip_1024", "mixed", 2), ("gain_ark4ip_1024", "mixed", 4),
     ("sc_blowwood_fixed_4096", "mixed", 1), ("ss_sym_rk4_sc_1024", "fp64", 2),
-    ("ss_sym_rk4_sc_1024", "mixed", 4), ("ss_sym_rk4_soliton_1024", "fp32", 2),
+    ("ss_sym_rk4_sc_1024", "mixed", 4), ("ss_sym_rk4_soliton_1024", "mixed", 2),
     ("ss_symmetric_sc_1024", "fp64", 2), ("ss_symmetric_sc_1024", "mixed", 4),
-    ("ss_symmetric_soliton_1024", "fp32", 2), ("yb_ark4ip_1024", "fp64", 2),
-    ("yb_ark4ip_1024", "mixed", 4), ("yb_ark4ip_1024", "fp32", 2), ("yb_fixed_2048", "fp64", 2)])
+    ("ss_symmetric_soliton_1024", "mixed", 2), ("yb_ark4ip_1024", "fp64", 2),
+    ("yb_ark4ip_1024", "mixed", 4), ("yb_fixed_2048", "fp32", 2), ("yb_fixed_2048", "fp64", 2)])
 def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     case = gc.load(name)
     _, out, st = run(case, precision, cluster)
