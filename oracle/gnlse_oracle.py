@@ -16,8 +16,10 @@ time-domain formulation of:
 * ``Linearity.default_linearity``/``default_exp_f[_cached]``
   (``pyofss/modules/linearity.py:162-186,241-272``);
 * ``Nonlinearity.__call__``, ``default_f_all``, ``default_f``,
-  ``default_f_with_ss`` and the Blow-Wood / Hollenbeck Raman responses
-  (``pyofss/modules/nonlinearity.py:53-100,160-207,213-220,266-267``);
+  ``default_f_with_ss``, the legacy ``rs_factor`` terms (``default_f_with_rs``,
+  ``default_f_with_ss_and_rs`` and their exponential forms) and the Blow-Wood /
+  Hollenbeck Raman responses
+  (``pyofss/modules/nonlinearity.py:53-100,160-207,213-270``);
 * ``Amplifier.factor`` with the Lorentzian gain profile
   (``pyofss/modules/amplifier.py:110-158``) and Simpson energy
   (``pyofss/field.py:161-172``);
@@ -231,10 +233,12 @@ class Nonlinear:
     """``Nonlinearity`` for the default single-channel model (nonlinearity.py:103-207)."""
 
     def __init__(self, grid, gamma, self_steepening=False, use_all=False, tau_1=12.2e-3,
-                 tau_2=32.0e-3, f_R=0.18):
+                 tau_2=32.0e-3, f_R=0.18, raman_scattering=False, rs_factor=3e-3):
         self.gamma = gamma
         self.f_R = f_R
         self.use_all = use_all
+        self.rs_on = bool(raman_scattering)
+        self.rs_factor = rs_factor
         self.omega = fftshift(grid.omega - grid.centre_omega)
         if self_steepening is False:
             self.ss_factor = 0.0
@@ -261,6 +265,15 @@ class Nonlinear:
             convolution = ifft(self.h_R * fft(term_spm))
             p = fft(A * (1.0 - self.f_R) * term_spm + self.f_R * A * convolution)
             return ifft(self.factor * (1.0 + self.omega * self.ss_factor) * p)
+        if self.rs_on:
+            # default_f_with_rs / default_f_with_ss_and_rs (nonlinearity.py:236-256); the
+            # latter adds its self-steepening term without the factor i gamma
+            term_spm = np.abs(A) ** 2
+            term_rs = self.rs_factor * ifft(1j * self.omega * fft(term_spm))
+            out = self.factor * (term_spm + term_rs) * A
+            if self.ss_on:
+                out = out + self.ss_factor * ifft(self.omega * fft(term_spm * A))
+            return out
         if self.ss_on:
             # default_f_with_ss (nonlinearity.py:209-214)
             term_spm = np.abs(A) ** 2 * A
@@ -280,6 +293,14 @@ class Nonlinear:
                 inv_b = np.where(np.abs(B) > 1e-15, self.ss_factor / B, 0.0)
             term_ss_all = inv_b * ifft(self.omega * fft(term_all * A))
             return np.exp(h * self.factor * (term_all + term_ss_all)) * B
+        if self.rs_on:
+            # default_exp_f_with_rs / default_exp_f_with_ss_and_rs (nonlinearity.py:243-264)
+            term_spm = np.abs(A) ** 2
+            term_rs = self.rs_factor * ifft(1j * self.omega * fft(term_spm))
+            if self.ss_on:
+                term_ss = (self.ss_factor / B) * ifft(self.omega * fft(term_spm * A))
+                return np.exp(h * self.factor * (term_spm + term_ss + term_rs)) * B
+            return np.exp(h * self.factor * (term_spm + term_rs)) * B
         if self.ss_on:
             # default_exp_f_with_ss (nonlinearity.py:230-234)
             term_spm = np.abs(A) ** 2
@@ -425,12 +446,14 @@ class Propagator:
 
     def __init__(self, grid, length, beta=None, alpha=None, gamma=0.0, self_steepening=False,
                  use_all=False, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18, centre_omega=None,
+                 raman_scattering=False, rs_factor=3e-3,
                  small_signal_gain=None, E_sat=None, lamb0=None, bandwidth=None,
                  use_Yb_model=False, Pp_0=None, N=None, Rr=None, yb_cross_sections=None):
         self.grid = grid
         self.length = length
         self.factor = linear_factor(grid, beta, alpha, centre_omega)
-        self.nl = Nonlinear(grid, gamma, self_steepening, use_all, tau_1, tau_2, f_R)
+        self.nl = Nonlinear(grid, gamma, self_steepening, use_all, tau_1, tau_2, f_R,
+                            raman_scattering, rs_factor)
         self.gain = None
         if use_Yb_model:  # fibre.py:97-103: the Yb model replaces the saturable amplifier
             s12, s21 = yb_cross_sections

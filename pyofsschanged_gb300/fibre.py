@@ -14,9 +14,10 @@ pyofss/modules/stepper.py:33-47 are raised with the same names.
 
 The saturable amplifier and the Yb two-level gain (``use_Yb_model``; its cross
 sections from ``yb_cross_sections`` or an importable pyofss installation, its pump
-power after the run in ``fibre.amplifier.Pp``) run with the RK4IP methods.  Models
-outside the CUDA path (WDM two-channel, the legacy ``raman_scattering`` rs_factor
-terms, the Er gain profile, ASE noise) raise ``NotImplementedError``.
+power after the run in ``fibre.amplifier.Pp``) run with the RK4IP methods, and the
+legacy ``raman_scattering`` rs_factor term without self-steepening with every method.
+Models outside the CUDA path (WDM two-channel, the rs_factor term with self-steepening,
+the Er gain profile, ASE noise) raise ``NotImplementedError``.
 """
 
 import numpy as np
@@ -126,8 +127,9 @@ class Fibre:
                 f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4 / ss_symmetric")
         if sim_type not in (None, "default"):
             raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
-        if raman_scattering and not use_all:
-            raise NotImplementedError("legacy rs_factor Raman model is not on the CUDA path")
+        if raman_scattering and not use_all and self_steepening:
+            raise NotImplementedError("the legacy rs_factor Raman term with self-steepening is not on "
+                                      "the CUDA path")
         if use_Er_profile or use_Er_noise:
             raise NotImplementedError("the Er gain profile and ASE noise are not on the CUDA path")
         if use_Yb_model and m in ("ss_sym_rk4", "ss_symmetric"):
@@ -141,6 +143,7 @@ class Fibre:
         self.alpha, self.beta, self.gamma = alpha, beta, gamma
         self.self_steepening, self.use_all = self_steepening, use_all
         self.tau_1, self.tau_2, self.f_R = tau_1, tau_2, f_R
+        self.raman_scattering, self.rs_factor = raman_scattering, rs_factor
         self.centre_omega = centre_omega
         self.small_signal_gain, self.E_sat = small_signal_gain, E_sat
         self.lamb0, self.bandwidth = lamb0, bandwidth
@@ -159,6 +162,7 @@ class Fibre:
         g = GridTables(domain, beta=self.beta, alpha=self.alpha, gamma=self.gamma,
                        self_steepening=self.self_steepening, use_all=self.use_all,
                        tau_1=self.tau_1, tau_2=self.tau_2, f_R=self.f_R,
+                       raman_scattering=self.raman_scattering, rs_factor=self.rs_factor,
                        centre_omega=self.centre_omega, small_signal_gain=self.small_signal_gain,
                        E_sat=self.E_sat, length=self.length, lamb0=self.lamb0,
                        bandwidth=self.bandwidth, use_Yb_model=self.use_Yb_model, Pp_0=self.Pp_0,

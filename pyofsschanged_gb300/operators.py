@@ -12,7 +12,9 @@ These are the tables pyofss builds once per domain:
   Lorentzian profile ``1 / (1 + 4 (nu - nu0)^2 / dnu^2)`` with
   ``dnu = c bandwidth / lamb0^2`` in FFT order (``Amplifier``, amplifier.py:57-158);
 * the Yb two-level gain (``Amplifier2LevelModel``, amplifier.py:178-379): the
-  per-frequency gain and inversion tables and the pump constants.
+  per-frequency gain and inversion tables and the pump constants;
+* the legacy Raman term ``rs_factor d|A|^2/dt`` (``raman_scattering`` without
+  ``use_all``, nonlinearity.py:236-248), as an equivalent response table.
 """
 
 import importlib.util
@@ -215,7 +217,7 @@ class GridTables:
                  use_all=False, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18, centre_omega=None,
                  small_signal_gain=None, E_sat=None, length=1.0, lamb0=None, bandwidth=None,
                  use_Yb_model=False, Pp_0=None, N=None, Rr=None, yb_cross_sections=None,
-                 cluster=0):
+                 raman_scattering=False, rs_factor=3e-3, cluster=0):
         self.domain = domain
         self.n = domain.total_samples
         self.dt = float(domain.dt)
@@ -228,6 +230,19 @@ class GridTables:
         self.ss_w = np.ascontiguousarray(1.0 + omega * s, float) if s != 0.0 else None
         hr = raman_spectrum(domain, use_all, tau_1, tau_2)
         self.f_R = float(f_R) if hr is not None else 0.0
+        if raman_scattering and not use_all:
+            # The legacy term (default_f_with_rs, nonlinearity.py:236-248):
+            # i gamma (|x|^2 + rs ifft(i omega fft(|x|^2))) x.  The engine evaluates
+            # i gamma' ((1 - f_R)|x|^2 + f_R ifft(hR/n ... )) x with hR = fft(h_R) window_t;
+            # hR = i rs omega, f_R = 1/2 and gamma' = 2 gamma give the same term (the
+            # factors 1/2 and 2 are exact in floating point).
+            if s != 0.0:
+                raise NotImplementedError(
+                    "raman_scattering with self_steepening: the reference adds that self-steepening "
+                    "term without the factor i gamma (nonlinearity.py:250-256); not on the CUDA path")
+            hr = 1j * float(rs_factor) * omega
+            self.f_R = 0.5
+            self.gamma = 2.0 * self.gamma
         self.hR_re = None if hr is None else np.ascontiguousarray(hr.real, float)
         self.hR_im = None if hr is None else np.ascontiguousarray(hr.imag, float)
         self.nu = np.ascontiguousarray(fftshift(domain.nu), float)

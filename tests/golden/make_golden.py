@@ -131,6 +131,18 @@ CASES = {
         fibre=dict(length=3.0e-4, beta=[0.0, 0.0, 25.0, 0.05], gamma=5.0,
                    use_Yb_model=True, Pp_0=5.0, N=5.0, Rr=1.0e-5, method="rk4ip",
                    total_steps=200, traces=4)),
+    # The legacy Raman term rs_factor d|A|^2/dt (raman_scattering=True without use_all,
+    # nonlinearity.py:236-248): adaptive RK4IP and the exponential split step.
+    "rs_ark4ip_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=1.0e-5, beta=BETA_SC, gamma=110.0, raman_scattering=True,
+                   rs_factor=3.0e-3, method="ark4ip", local_error=1e-6, traces=1)),
+    "rs_ss_symmetric_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, raman_scattering=True,
+                   rs_factor=3.0e-3, method="ss_symmetric", total_steps=800, traces=1)),
 }
 
 SLOW = {"sc_cfg_8192"}

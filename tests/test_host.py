@@ -158,3 +158,25 @@ def test_yb_cross_section_table_reading(tmp_path):
     np.testing.assert_allclose(amp.sigma12_s, o12, rtol=1e-14, atol=0)
     np.testing.assert_allclose(amp.sigma21_s, o21, rtol=1e-14, atol=0)
     assert np.all(amp.sigma12_s[d.Lambda > 1060.0] == 0.0)
+
+
+def test_rs_factor_tables_reproduce_the_reference_term():
+    """raman_scattering=True (nonlinearity.py:236-248) as the engine's Raman tables: the
+    engine's term i gamma' ((1 - f_R)|x|^2 + f_R ifft(hR fft(|x|^2))) x equals the
+    oracle's default_f_with_rs term."""
+    case = gc.load("rs_ark4ip_1024")
+    prm = case["params"]
+    fk = gc.fibre_kwargs(prm)
+    d = Domain(**gc.domain_kwargs(prm))
+    g = GridTables(d, beta=fk["beta"], gamma=fk["gamma"], raman_scattering=True,
+                   rs_factor=fk["rs_factor"])
+    nl = go.Nonlinear(go.Grid(**gc.domain_kwargs(prm)), fk["gamma"], raman_scattering=True,
+                      rs_factor=fk["rs_factor"])
+    x = case["A0"]
+    p = np.abs(x) ** 2
+    hr = g.hR_re + 1j * g.hR_im
+    conv = go.ifft(hr * go.fft(p))  # G-(hR/n G+(p)) in pyofss fft terms
+    engine_term = 1j * g.gamma * ((1.0 - g.f_R) * p + g.f_R * conv) * x
+    np.testing.assert_allclose(engine_term, nl(x), rtol=1e-12, atol=1e-9 * np.abs(nl(x)).max())
+    with pytest.raises(NotImplementedError):
+        GridTables(d, beta=fk["beta"], gamma=fk["gamma"], raman_scattering=True, self_steepening=True)
