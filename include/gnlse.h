@@ -69,7 +69,13 @@ enum {
  * evaluated with the unpropagated field, linear half step; not with self-steepening,
  * whose exponent in the reference divides by the field).  Neither split step runs with
  * gain or the Yb model (GNLSE_UNSUPPORTED). */
-enum { GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2, GNLSE_SS_SYMMETRIC = 3 };
+enum {
+  GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2, GNLSE_SS_SYMMETRIC = 3,
+  GNLSE_SS_SIMPLE = 4,  /* Solver.ss_simple (solver.py:256-265): exponential nonlinear step, then a
+                           full linear step; fixed step, no gain, no self-steepening */
+  GNLSE_SS_REDUCED = 5  /* Solver.ss_reduced (solver.py:277-287): ss_symmetric with the exponent
+                           from the half-step-propagated field; same limits */
+};
 /* precision: GNLSE_FP32 complex64 throughout (fields complex64);
  * GNLSE_FP64 complex128 throughout (fields complex128);
  * GNLSE_MIXED complex64 transforms and nonlinear evaluations with the
@@ -120,7 +126,7 @@ typedef struct {
 /* One propagation (one field through one fibre). */
 typedef struct {
   int32_t grid;               /* index into the grid array */
-  int32_t method;             /* GNLSE_RK4IP / GNLSE_SS_SYM_RK4 / GNLSE_SS_SYMMETRIC (fixed step), GNLSE_ARK4IP */
+  int32_t method;             /* GNLSE_RK4IP / GNLSE_SS_* (fixed step), GNLSE_ARK4IP */
   int32_t total_steps;        /* Fibre total_steps */
   int32_t traces;             /* Fibre traces (>= 1) */
   int32_t max_traces;         /* trace slots reserved for this instance (0: none) */

@@ -24,7 +24,8 @@ time-domain formulation of:
   (``pyofss/modules/amplifier.py:110-158``) and Simpson energy
   (``pyofss/field.py:161-172``);
 * the Yb two-level gain ``Amplifier2LevelModel`` (``pyofss/modules/amplifier.py:178-379``);
-* ``Solver.rk4ip`` (``pyofss/modules/solver.py:339-354``);
+* ``Solver.rk4ip`` (``pyofss/modules/solver.py:339-354``) and the split-step methods
+  ``ss_simple``, ``ss_symmetric``, ``ss_reduced``, ``ss_sym_rk4`` (``solver.py:256-287,330-337``);
 * ``Stepper.standard_stepper`` / ``adaptive_stepper`` / ``relative_local_error``
   (``pyofss/modules/stepper.py:164-221,231-376``).
 
@@ -502,6 +503,21 @@ class Propagator:
         A_N = self.nl.exp_non(A, h, A_L)
         return self.linear(A_N, 0.5 * h)
 
+    def ss_simple(self, A, h):
+        """``Solver.ss_simple`` (solver.py:256-265): exponential nonlinear step with the
+        field itself, then a full linear step."""
+        self.evals += 1
+        A_N = self.nl.exp_non(A, h, A)
+        return self.linear(A_N, h)
+
+    def ss_reduced(self, A, h):
+        """``Solver.ss_reduced`` (solver.py:277-287): linear half step, exponential
+        nonlinear step with the propagated field, linear half step."""
+        self.evals += 1
+        A_L = self.linear(A, 0.5 * h)
+        A_N = self.nl.exp_non(A_L, h, A_L)
+        return self.linear(A_N, 0.5 * h)
+
     def ss_sym_rk4(self, A, h):
         """``Solver.ss_sym_rk4`` (solver.py:330-337): linear half step, classical RK4 on
         the nonlinear term, linear half step."""
@@ -516,7 +532,8 @@ class Propagator:
         zs = np.linspace(0.0, self.length, total_steps + 1)
         storage_step = int(total_steps / traces)
         trace_z, trace_A = [], []
-        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric}[method]
+        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric,
+                "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced}[method]
         for i, z in enumerate(zs[:-1]):
             A = step(A, h)
             if traces != 1 and i % storage_step == 0:

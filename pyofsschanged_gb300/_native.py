@@ -25,6 +25,8 @@ GNLSE_RK4IP = 0
 GNLSE_ARK4IP = 1
 GNLSE_SS_SYM_RK4 = 2
 GNLSE_SS_SYMMETRIC = 3
+GNLSE_SS_SIMPLE = 4
+GNLSE_SS_REDUCED = 5
 GNLSE_FP32 = 0
 GNLSE_FP64 = 1
 GNLSE_MIXED = 2

@@ -452,19 +452,18 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   for (int i = 0; i < n_instances; ++i) {
     const gnlse_instance_desc& id = instances[i];
     if (id.grid < 0 || id.grid >= n_grids ||
-        (id.method != GNLSE_RK4IP && id.method != GNLSE_ARK4IP && id.method != GNLSE_SS_SYM_RK4 &&
-         id.method != GNLSE_SS_SYMMETRIC) ||
+        id.method < GNLSE_RK4IP || id.method > GNLSE_SS_REDUCED ||
         id.total_steps < 1 || id.traces < 1 || id.max_traces < 0 || !(id.length >= 0) ||
         (id.method == GNLSE_ARK4IP && !(id.local_error > 0))) {
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
-    if ((id.method == GNLSE_SS_SYM_RK4 || id.method == GNLSE_SS_SYMMETRIC) &&
-        (grids[id.grid].gain_on || grids[id.grid].yb_on)) {
+    const bool split = id.method >= GNLSE_SS_SYM_RK4;
+    if (split && (grids[id.grid].gain_on || grids[id.grid].yb_on)) {
       free_plan(p);  // the split-step paths have no amplifier step
       return GNLSE_UNSUPPORTED;
     }
-    if (id.method == GNLSE_SS_SYMMETRIC && grids[id.grid].ss_w) {
+    if (id.method >= GNLSE_SS_SYMMETRIC && grids[id.grid].ss_w) {
       free_plan(p);  // exponential step with self-steepening (see gnlse.h)
       return GNLSE_UNSUPPORTED;
     }

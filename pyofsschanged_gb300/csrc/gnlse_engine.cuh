@@ -1011,16 +1011,20 @@ struct Engine {
     __syncthreads();
   }
 
-  // One step of Solver.ss_symmetric (solver.py:267-275) without self-steepening:
-  //   S_L = E S                                   (linear half step, E = exp(hD/2))
-  //   B = G-(S_L)/N, a = G-(S)/N                  (time domain; B kept in global Bt)
+  // One step of the exponential split-step methods without self-steepening:
+  //   S_L = E1 S                                  (first linear step)
+  //   B = G-(S_L)/N, a = G-(S or S_L)/N           (time domain; B kept in global Bt)
   //   t = (1 - fR)|a|^2 + fR G-(Hp G+(|a|^2))     (or |a|^2; default_exp_f[_all],
   //                                                 nonlinearity.py:209-221,269-270)
-  //   A_N = exp(i gamma h t) B ;  S' = E G+(A_N)  (linear half step)
-  // computed as S' = E (S_L + G+((exp(i gamma h t) - 1) B)), which keeps the
+  //   A_N = exp(i gamma h t) B ;  S' = E2 G+(A_N) (second linear step)
+  // computed as S' = E2 (S_L + G+((exp(i gamma h t) - 1) B)), which keeps the
   // propagation state's precision when the nonlinear phase per step is small.
+  //   Solver.ss_symmetric (solver.py:267-275): E1 = E2 = exp(hD/2), a from S
+  //   Solver.ss_reduced   (solver.py:277-287): E1 = E2 = exp(hD/2), a from S_L
+  //   Solver.ss_simple    (solver.py:256-265): E1 = 1, E2 = exp(hD), a from S
   static __device__ __forceinline__ void ss_symmetric_step(const Ctx& cx, const GridDev& g, const SV* S, SV* Sh,
-                                                        V* Bt, const SV* E, double h) {
+                                                        V* Bt, const SV* E, const SV* E2, double h,
+                                                        bool t_from_sl) {
     const R invN = (R)(1.0 / (double)N);
     const int base = cx.rank * M;
     V* X = cx.X;
@@ -1040,14 +1044,15 @@ struct Engine {
     auto rdSh = [&](int o, int l) -> V { return ldv(Sh, o * M + l); };
     auto wrB = [&](int n1, int n2, V v) { Bt[n1 * M + n2] = cscale(v, invN); };
     inv(cx, X, rdSh, wrB);  // B = G-(S_L)/N
-    auto rdS = [&](int o, int l) -> V { return ldv(S, o * M + l); };
+    const SV* Sa = t_from_sl ? Sh : S;
+    auto rdS = [&](int o, int l) -> V { return ldv(Sa, o * M + l); };
     auto e1 = [&](int n1, int n2, V v) {
       const int sl = pad(tslot(n1, n2));
       const V x = cscale(v, invN);
       X[sl] = x;
       P[sl] = mk<V>(cabs2(x), (R)0);
     };
-    inv(cx, X, rdS, e1);  // a = G-(S)/N, |a|^2
+    inv(cx, X, rdS, e1);  // a = G-(S or S_L)/N, |a|^2
     if (g.raman) {
       const V* Hp = (const V*)g.Hp;
       const R fR = (R)g.fR, f1 = (R)(1.0 - g.fR);
@@ -1080,14 +1085,14 @@ struct Engine {
       X[pad(l)] = cmul(ephi, b);
     }
     __syncthreads();
-    // S' = E (S_L + G+(Delta))
+    // S' = E2 (S_L + G+(Delta))
     auto rdXt = [&](int n1, int n2) -> V { return X[pad(tslot(n1, n2))]; };
     auto wrS = [&](int, int l, V v) {
       const int a = base + l;
       if constexpr (XS) {
-        dfc_store(Sh, a, dfc_mul(dfc_load(E, a), dfc_add_f(dfc_load(Sh, a), v)));
+        dfc_store(Sh, a, dfc_mul(dfc_load(E2, a), dfc_add_f(dfc_load(Sh, a), v)));
       } else {
-        Sh[a] = cmul(E[a], cadd(Sh[a], v));
+        Sh[a] = cmul(E2[a], cadd(Sh[a], v));
       }
     };
     fwd(cx, X, rdXt, wrS);
@@ -1349,10 +1354,13 @@ struct Engine {
     // term (the RK4IP stage algebra with the exp(hD/2) factors replaced by an exact 1,
     // table 6), result <- E result, E = exp(hD/2) (table 7)
     const bool ssrk = d.method == 2;
-    const bool sssym = d.method == 3;  // Solver.ss_symmetric, ss_symmetric_step
+    // Solver.ss_symmetric (3), ss_simple (4), ss_reduced (5): ss_symmetric_step
+    const bool sssym = d.method >= 3;
+    const bool sssimple = d.method == 4;
     if (st.phase == 1 && !adaptive) {
-      exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
-      if (ssrk) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
+      // exp(hD/2), or exp(hD) for ss_simple, whose one linear step spans the step
+      exp_table(cx, g, (sssimple ? 1.0 : 0.5) * (d.length / d.total_steps), base + 7 * N, nullptr);
+      if (ssrk || sssimple) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
     }
 
     // Solver.ss_symmetric: a step loop of its own, so that the main loop below keeps
@@ -1361,7 +1369,8 @@ struct Engine {
       const double h = d.length / d.total_steps;
       const int sidx = st.sidx;
       ss_symmetric_step(cx, g, base + (long long)sidx * N, base + (long long)(sidx ^ 1) * N,
-                        reinterpret_cast<V*>(base + 2 * N), base + 7 * N, h);
+                        reinterpret_cast<V*>(base + 2 * N), base + (sssimple ? 6 : 7) * N, base + 7 * N, h,
+                        d.method == 5);
       if (threadIdx.x == 0) st.evals += 1;
       budget -= 1;
       fixed_step_done(cx, kp, c, base, h);

@@ -16,7 +16,8 @@ from . import _native as nat
 
 PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE_MIXED}
 METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP, "ss_sym_rk4": nat.GNLSE_SS_SYM_RK4,
-           "ss_symmetric": nat.GNLSE_SS_SYMMETRIC}
+           "ss_symmetric": nat.GNLSE_SS_SYMMETRIC, "ss_simple": nat.GNLSE_SS_SIMPLE,
+           "ss_reduced": nat.GNLSE_SS_REDUCED}
 
 
 def _ptr(a):
@@ -34,7 +35,7 @@ class Instance:
         self.weight = float(weight)
         self.method = method.lower()
         if self.method not in METHODS:
-            raise ValueError(f"unknown method {method!r} (rk4ip, ark4ip, ss_sym_rk4 or ss_symmetric)")
+            raise ValueError(f"unknown method {method!r} ({', '.join(METHODS)})")
         self.length = float(length)
         self.local_error = float(local_error)
         self.total_steps = int(total_steps)
@@ -42,7 +43,7 @@ class Instance:
         if max_traces is None:
             if self.traces == 1:
                 max_traces = 0
-            elif self.method in ("rk4ip", "ss_sym_rk4", "ss_symmetric"):  # fixed-step trace rule
+            elif self.method != "ark4ip":  # fixed-step trace rule
                 step = self.total_steps // self.traces if self.traces else 0
                 max_traces = (self.total_steps + step - 1) // step if step > 0 else 0
             else:

@@ -6,8 +6,8 @@ propagates the field through the fibre and returns it, as
 ``Fibre.__call__`` does (fibre.py:136-148).  ``method`` selects the engine
 path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps),
 ``"cuda_ark4ip"`` / ``"ark4ip"`` (adaptive step doubling with tolerance
-``local_error``), or the fixed-step split-step methods ``"ss_sym_rk4"`` and
-``"ss_symmetric"`` (pyofss/modules/solver.py:267-275,330-337).  ``precision`` selects ``"mixed"`` (default: complex64
+``local_error``), or the fixed-step split-step methods ``"ss_sym_rk4"``,
+``"ss_symmetric"``, ``"ss_simple"`` and ``"ss_reduced"`` (pyofss/modules/solver.py:256-287,330-337).  ``precision`` selects ``"mixed"`` (default: complex64
 transforms with a double-float propagation state), ``"fp32"`` (complex64
 throughout) or ``"fp64"`` (complex128 throughout).  The stepper exceptions of
 pyofss/modules/stepper.py:33-47 are raised with the same names.
@@ -122,9 +122,10 @@ class Fibre:
         m = method.lower()
         if m.startswith("cuda_"):
             m = m[5:]
-        if m not in ("rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric"):
+        if m not in ("rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric", "ss_simple", "ss_reduced"):
             raise NotImplementedError(
-                f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4 / ss_symmetric")
+                f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4 / ss_symmetric / "
+                "ss_simple / ss_reduced")
         if sim_type not in (None, "default"):
             raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
         if raman_scattering and not use_all and self_steepening:
@@ -132,7 +133,7 @@ class Fibre:
                                       "the CUDA path")
         if use_Er_profile or use_Er_noise:
             raise NotImplementedError("the Er gain profile and ASE noise are not on the CUDA path")
-        if use_Yb_model and m in ("ss_sym_rk4", "ss_symmetric"):
+        if use_Yb_model and m.startswith("ss_"):
             raise NotImplementedError("the split-step methods run without gain on the CUDA path")
         if small_signal_gain is not None and E_sat is None and P_sat is not None:
             if Tr is None:

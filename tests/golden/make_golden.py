@@ -143,6 +143,18 @@ CASES = {
         pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
         fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, raman_scattering=True,
                    rs_factor=3.0e-3, method="ss_symmetric", total_steps=800, traces=1)),
+    # Simple and reduced split steps (solver.py:256-287): SPM soliton and Raman.
+    "ss_simple_soliton_1024": dict(
+        domain=dict(bit_width=32.0, samples_per_bit=1024, centre_nu=193.1),
+        pulse=dict(kind="sech", peak_power=80.0, width=1.0),
+        fibre=dict(length=np.pi / 20, beta=[0.0, 0.0, -20.0], gamma=1.0, method="ss_simple",
+                   total_steps=2000, traces=10)),
+    "ss_reduced_sc_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
+                   use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
+                   method="ss_reduced", total_steps=800, traces=1)),
 }
 
 SLOW = {"sc_cfg_8192"}

@@ -47,6 +47,6 @@ def expected_evals(case):
     """Solver evaluations of the reference run: its logged rk4ip calls, or one per fixed
     step for the split-step method (which makes no rk4ip calls)."""
     fk = case["params"]["fibre"]
-    if fk["method"] in ("ss_sym_rk4", "ss_symmetric"):
+    if fk["method"].startswith("ss_"):
         return fk["total_steps"]
     return len(case["rk4ip_calls"])

@@ -85,7 +85,8 @@ def test_fp32_matches_reference(cuda_ready, name):
     case = gc.load(name)
     plan, out, st = run(case, "fp32")
     assert st["status"] == 0 and st["finished"] == 1
-    tol = 1e-3 if name in CHAOTIC else (FP32_SPLIT_STEP_TOL if name.startswith("ss_") else FP32_SPEC_TOL)
+    split = case["params"]["fibre"]["method"].startswith("ss_")
+    tol = 1e-3 if name in CHAOTIC else (FP32_SPLIT_STEP_TOL if split else FP32_SPEC_TOL)
     assert spec_err(out, case["A_out"]) <= tol
     # the step-size controller sees FP32 round-off; the attempt count stays close
     # (within 6%: the Yb gain run takes 4 attempts more than the reference's 72)
@@ -104,7 +105,9 @@ def test_fp32_matches_reference(cuda_ready, name):
     ("ss_sym_rk4_sc_1024", "mixed", 4), ("ss_sym_rk4_soliton_1024", "mixed", 2),
     ("ss_symmetric_sc_1024", "fp64", 2), ("ss_symmetric_sc_1024", "mixed", 4),
     ("ss_symmetric_soliton_1024", "mixed", 2), ("yb_ark4ip_1024", "fp64", 2),
-    ("yb_ark4ip_1024", "mixed", 4), ("yb_fixed_2048", "fp32", 2), ("yb_fixed_2048", "fp64", 2)])
+    ("yb_ark4ip_1024", "mixed", 4), ("yb_fixed_2048", "fp32", 2), ("yb_fixed_2048", "fp64", 2),
+    ("ss_simple_soliton_1024", "fp64", 2), ("ss_reduced_sc_1024", "mixed", 4),
+    ("rs_ark4ip_1024", "fp64", 2), ("rs_ss_symmetric_1024", "mixed", 2)])
 def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     case = gc.load(name)
     _, out, st = run(case, precision, cluster)
@@ -115,8 +118,8 @@ def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     elif precision == "mixed":
         assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
     else:
-        assert spec_err(out, case["A_out"]) <= (FP32_SPLIT_STEP_TOL if name.startswith("ss_")
-                                                 else FP32_SPEC_TOL)
+        split = case["params"]["fibre"]["method"].startswith("ss_")
+        assert spec_err(out, case["A_out"]) <= (FP32_SPLIT_STEP_TOL if split else FP32_SPEC_TOL)
 
 
 @pytest.mark.parametrize("name", ["yb_ark4ip_1024", "yb_fixed_2048"])
