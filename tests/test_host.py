@@ -180,3 +180,21 @@ def test_rs_factor_tables_reproduce_the_reference_term():
     np.testing.assert_allclose(engine_term, nl(x), rtol=1e-12, atol=1e-9 * np.abs(nl(x)).max())
     with pytest.raises(NotImplementedError):
         GridTables(d, beta=fk["beta"], gamma=fk["gamma"], raman_scattering=True, self_steepening=True)
+
+
+def test_fibre_model_options_on_the_cuda_path():
+    """Fibre accepts the models the engine runs and refuses the rest at construction."""
+    from pyofsschanged_gb300 import Fibre
+    Fibre(length=1e-5, beta=[0, 0, -10.0], gamma=100.0, raman_scattering=True, method="cuda_ark4ip")
+    Fibre(length=1e-3, beta=[0, 0, 25.0], gamma=5.0, use_Yb_model=True, Pp_0=1.0, N=1.0, Rr=1e-5,
+          method="cuda_rk4ip")
+    for m in ("ss_simple", "ss_reduced", "ss_symmetric", "ss_sym_rk4"):
+        Fibre(length=1e-5, beta=[0, 0, -10.0], gamma=100.0, method=m)
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-5, gamma=100.0, raman_scattering=True, self_steepening=True)
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, use_Yb_model=True, Pp_0=1.0, N=1.0, Rr=1e-5, method="ss_simple")
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, use_Er_profile=True)
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, method="ss_agrawal")
