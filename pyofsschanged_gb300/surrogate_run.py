@@ -7,7 +7,7 @@
    +-500 fs^2) on the 2^13-point 835 nm grid;
 2. their propagation through 5 cm of the supercontinuum fibre by the batched
    RK4IP engine (ARK4IP 1e-6, mixed precision) -- training data, calibration
-   data and the test set's reference ("the judge");
+   data and the reference outputs of the test set;
 3. two networks trained from different seeds on the training split; the error
    estimate's scale calibrated on the calibration split;
 4. the test set through the surrogate with RK4IP fallback at the tolerance:
