@@ -128,6 +128,20 @@ def load_costs(n_members):
     return [r["attempts"] for r in res[:n_members]], [r["n"] for r in res[:n_members]]
 
 
+def spectral_power_db_error(out_t, ref_t, floor_db=-40.0):
+    """Largest |10 log10(P_out / P_ref)| over the spectral bins within ``floor_db`` of the
+    reference spectrum's peak (P = |fft(A)|^2 of the time-domain fields), in dB."""
+    import numpy as np
+    p_ref = np.abs(np.fft.ifft(ref_t)) ** 2
+    p_out = np.abs(np.fft.ifft(out_t)) ** 2
+    band = p_ref >= p_ref.max() * 10.0 ** (floor_db / 10.0)
+    if not band.any():
+        return 0.0
+    with np.errstate(divide="ignore"):
+        d = 10.0 * np.log10(np.maximum(p_out[band], 1e-300) / p_ref[band])
+    return float(np.max(np.abs(d)))
+
+
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -379,14 +393,16 @@ def run_ours(a):
         p64.propagate(f64)
         ref = [x.cpu().numpy() for x in p64.unpack(f64)]
         out = [x.cpu().numpy().astype(complex) for x in plan.unpack(work)]
-        errs = []
+        errs, db_errs = [], []
         for j, i in enumerate(idx):
             s_ref = np.fft.ifft(ref[j])
             s_out = np.fft.ifft(out[i])
             errs.append(float(np.linalg.norm(s_out - s_ref) / np.linalg.norm(s_ref)))
+            db_errs.append(spectral_power_db_error(out[i], ref[j]))
         acc = {"members": len(idx), "median": statistics.median(errs), "max": max(errs),
                "frac_le_1e-4": sum(e <= 1e-4 for e in errs) / len(errs),
-               "per_member": [float("%.3e" % e) for e in errs]}
+               "per_member": [float("%.3e" % e) for e in errs],
+               "spectral_power_db_max_within_40db": [float("%.3e" % e) for e in db_errs]}
         # conditioning of the same members: the FP64 oracle's output change when only
         # the input is rounded to complex64 (tests/golden/make_ensemble_conditioning.py)
         try:
