@@ -1,0 +1,37 @@
+"""Register budget of the ensemble's hot kernel classes (compile only, no GPU).
+
+The mixed-precision cluster classes are bound by latency at 4 CTAs per SM, and their
+speed follows their local-memory traffic: a code path that never runs in an RK4IP
+propagation (a call to a separate function from the stage loop, a second step loop)
+can still raise the spills of the loop.  ptxas's resource report (-Xptxas -v) of the
+two classes that dominate the ensemble benchmark guards against that."""
+
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "pyofsschanged_gb300", "csrc")
+
+pytestmark = pytest.mark.skipif(shutil.which("nvcc") is None, reason="no nvcc")
+
+# (unit, most registers, most spill-store bytes of the kernel entry)
+BUDGET = [("gnlse_inst_mix_m11_c8.cu", 128, 720), ("gnlse_inst_mix_m12_c1.cu", 128, 64)]
+
+
+@pytest.mark.parametrize("unit,max_regs,max_spill", BUDGET)
+def test_hot_class_register_budget(tmp_path, unit, max_regs, max_spill):
+    out = subprocess.run(
+        ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+         "--expt-relaxed-constexpr", "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-Xptxas", "-v",
+         "-c", os.path.join(CSRC, unit), "-o", str(tmp_path / "unit.o")],
+        check=True, capture_output=True, text=True).stderr
+    lines = out.splitlines()
+    i = next(k for k, ln in enumerate(lines) if "Function properties for _ZN5gnlse12gnlse_kernel" in ln)
+    spill = int(re.search(r"(\d+) bytes spill stores", lines[i + 1]).group(1))
+    regs = int(re.search(r"Used (\d+) registers", lines[i + 2]).group(1))
+    assert regs <= max_regs, lines[i + 2]
+    assert spill <= max_spill, lines[i + 1]
