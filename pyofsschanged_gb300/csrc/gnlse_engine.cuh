@@ -857,10 +857,8 @@ struct Engine {
 
   // Yb model inversion sums sum_k w_ratio |X_k|^2, sum_k w_sat |X_k|^2 of a spectrum
   // X = n fft(x) held in src (0: op.MA0, 1: op.acc, 2: the X buffer), over the cluster,
-  // into out[0..1] (shared memory; written by thread 0 before the closing barrier).
-  // Inlined: calls to a separate function from the stage loop, even ones that never run,
-  // constrain the loop's register allocation (the 4096-point one-CTA class spilled ~1 KB).
-  static __device__ __forceinline__ void yb_sums(const Ctx& cx, const GridDev& g, const Op& op, int src,
+  // into out[0..1] (shared memory; written by thread 0 before the closing barrier)
+  static __device__ __noinline__ void yb_sums(const Ctx& cx, const GridDev& g, const Op& op, int src,
                                               double* out) {
     const double2* w = (const double2*)g.ybw;
     const int base = cx.rank * M;
