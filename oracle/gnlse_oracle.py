@@ -25,7 +25,8 @@ time-domain formulation of:
   (``pyofss/field.py:161-172``);
 * the Yb two-level gain ``Amplifier2LevelModel`` (``pyofss/modules/amplifier.py:178-379``);
 * ``Solver.rk4ip`` (``pyofss/modules/solver.py:339-354``) and the split-step methods
-  ``ss_simple``, ``ss_symmetric``, ``ss_reduced``, ``ss_sym_rk4`` (``solver.py:256-287,330-337``);
+  ``ss_simple``, ``ss_symmetric``, ``ss_reduced``, ``ss_sym_midpoint``, ``ss_sym_rk4``
+  (``solver.py:101-106,256-287,323-337``);
 * ``Stepper.standard_stepper`` / ``adaptive_stepper`` / ``relative_local_error``
   (``pyofss/modules/stepper.py:164-221,231-376``).
 
@@ -518,6 +519,15 @@ class Propagator:
         A_N = self.nl.exp_non(A_L, h, A_L)
         return self.linear(A_N, 0.5 * h)
 
+    def ss_sym_midpoint(self, A, h):
+        """``Solver.ss_sym_midpoint`` (solver.py:323-328) with ``Solver.midpoint``
+        (solver.py:101-106) on the nonlinear term."""
+        self.evals += 1
+        A_L = self.linear(A, 0.5 * h)
+        k0 = h * self.n(A_L)
+        A_N = A_L + h * self.n(A_L + 0.5 * k0)
+        return self.linear(A_N, 0.5 * h)
+
     def ss_sym_rk4(self, A, h):
         """``Solver.ss_sym_rk4`` (solver.py:330-337): linear half step, classical RK4 on
         the nonlinear term, linear half step."""
@@ -533,7 +543,8 @@ class Propagator:
         storage_step = int(total_steps / traces)
         trace_z, trace_A = [], []
         step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric,
-                "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced}[method]
+                "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced,
+                "ss_sym_midpoint": self.ss_sym_midpoint}[method]
         for i, z in enumerate(zs[:-1]):
             A = step(A, h)
             if traces != 1 and i % storage_step == 0:

@@ -155,6 +155,19 @@ CASES = {
         fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
                    use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
                    method="ss_reduced", total_steps=800, traces=1)),
+    # Symmetric split step with the midpoint method on the nonlinear term
+    # (solver.py:323-328): Raman + self-steepening supercontinuum and the N=2 soliton.
+    "ss_sym_midpoint_sc_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=True,
+                   use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
+                   method="ss_sym_midpoint", total_steps=800, traces=1)),
+    "ss_sym_midpoint_soliton_1024": dict(
+        domain=dict(bit_width=32.0, samples_per_bit=1024, centre_nu=193.1),
+        pulse=dict(kind="sech", peak_power=80.0, width=1.0),
+        fibre=dict(length=np.pi / 20, beta=[0.0, 0.0, -20.0], gamma=1.0, method="ss_sym_midpoint",
+                   total_steps=1000, traces=5)),
 }
 
 SLOW = {"sc_cfg_8192"}

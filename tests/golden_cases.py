@@ -11,6 +11,15 @@ def names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
 
+# methods of the reference that the CUDA engine runs (the oracle restates more)
+ENGINE_METHODS = {"rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric", "ss_simple", "ss_reduced"}
+
+
+def engine_names():
+    """Golden cases whose method the engine runs."""
+    return [n for n in names() if load(n)["params"]["fibre"]["method"] in ENGINE_METHODS]
+
+
 def load(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     case = {k: z[k] for k in z.files if k != "params"}

@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-9
 FP32_SPEC_TOL = 1e-4
-FAST = [n for n in gc.names() if n != "sc_cfg_8192"]
+FAST = [n for n in gc.engine_names() if n != "sc_cfg_8192"]
 
 
 def rel_l2(a, b):

@@ -198,3 +198,8 @@ def test_fibre_model_options_on_the_cuda_path():
         Fibre(length=1e-3, gamma=5.0, use_Er_profile=True)
     with pytest.raises(NotImplementedError):
         Fibre(length=1e-3, gamma=5.0, method="ss_agrawal")
+
+
+def test_engine_method_list_matches_the_plan():
+    from pyofsschanged_gb300.engine import METHODS
+    assert gc.ENGINE_METHODS == set(METHODS)
