@@ -25,8 +25,8 @@ time-domain formulation of:
   (``pyofss/field.py:161-172``);
 * the Yb two-level gain ``Amplifier2LevelModel`` (``pyofss/modules/amplifier.py:178-379``);
 * ``Solver.rk4ip`` (``pyofss/modules/solver.py:339-354``) and the split-step methods
-  ``ss_simple``, ``ss_symmetric``, ``ss_reduced``, ``ss_sym_midpoint``, ``ss_sym_rk4``
-  (``solver.py:101-106,256-287,323-337``);
+  ``ss_simple``, ``ss_symmetric``, ``ss_reduced``, ``ss_agrawal``, ``ss_sym_midpoint``,
+  ``ss_sym_rk4`` (``solver.py:101-106,256-337``);
 * ``Stepper.standard_stepper`` / ``adaptive_stepper`` / ``relative_local_error``
   (``pyofss/modules/stepper.py:164-221,231-376``).
 
@@ -519,6 +519,23 @@ class Propagator:
         A_N = self.nl.exp_non(A_L, h, A_L)
         return self.linear(A_N, 0.5 * h)
 
+    def ss_agrawal(self, A, h):
+        """``Solver.ss_agrawal`` (solver.py:290-320): iterated symmetric split step with the
+        nonlinear exponent averaged over the step's ends, N(Y)/Y taken as 0 where
+        |Y| <= 1e-5."""
+        self.evals += 1
+
+        def ratio(Y):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                return np.where(np.abs(Y) > 1.0e-5, self.n(Y) / Y, 0.0)
+
+        A_L = self.linear(A, 0.5 * h)
+        r_A = ratio(A)
+        A_N1 = np.exp(0.5 * h * (ratio(A) + r_A)) * A_L
+        Y_1 = self.linear(A_N1, 0.5 * h)
+        A_N2 = np.exp(0.5 * h * (ratio(Y_1) + r_A)) * A_L
+        return self.linear(A_N2, 0.5 * h)
+
     def ss_sym_midpoint(self, A, h):
         """``Solver.ss_sym_midpoint`` (solver.py:323-328) with ``Solver.midpoint``
         (solver.py:101-106) on the nonlinear term."""
@@ -544,7 +561,7 @@ class Propagator:
         trace_z, trace_A = [], []
         step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric,
                 "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced,
-                "ss_sym_midpoint": self.ss_sym_midpoint}[method]
+                "ss_sym_midpoint": self.ss_sym_midpoint, "ss_agrawal": self.ss_agrawal}[method]
         for i, z in enumerate(zs[:-1]):
             A = step(A, h)
             if traces != 1 and i % storage_step == 0:

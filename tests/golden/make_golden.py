@@ -168,6 +168,19 @@ CASES = {
         pulse=dict(kind="sech", peak_power=80.0, width=1.0),
         fibre=dict(length=np.pi / 20, beta=[0.0, 0.0, -20.0], gamma=1.0, method="ss_sym_midpoint",
                    total_steps=1000, traces=5)),
+    # Agrawal's iterated split step (solver.py:290-320): the N=2 soliton and a Raman
+    # supercontinuum without self-steepening.
+    "ss_agrawal_soliton_1024": dict(
+        domain=dict(bit_width=32.0, samples_per_bit=1024, centre_nu=193.1),
+        pulse=dict(kind="sech", peak_power=80.0, width=1.0),
+        fibre=dict(length=np.pi / 20, beta=[0.0, 0.0, -20.0], gamma=1.0, method="ss_agrawal",
+                   total_steps=1000, traces=1)),
+    "ss_agrawal_sc_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
+                   use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
+                   method="ss_agrawal", total_steps=800, traces=1)),
 }
 
 SLOW = {"sc_cfg_8192"}
