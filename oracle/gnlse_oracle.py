@@ -445,6 +445,9 @@ class Propagator:
     STEP_SIZE_MIN = 1e-37      # stepper.py:131
     SAFETY, MAX_FACTOR, MIN_FACTOR = 0.9, 10.0, 0.2  # stepper.py:133-135
     ETA = 5                    # solver.py:71
+    # Solver.errors (solver.py:57-70): the order used by the adaptive driver per method
+    ERRORS = {"rk4ip": 5, "ss_simple": 2, "ss_symmetric": 3, "ss_reduced": 2, "ss_agrawal": 3,
+              "ss_sym_midpoint": 3, "ss_sym_rk4": 5}
 
     def __init__(self, grid, length, beta=None, alpha=None, gamma=0.0, self_steepening=False,
                  use_all=False, tau_1=12.2e-3, tau_2=32.0e-3, f_R=0.18, centre_omega=None,
@@ -559,9 +562,7 @@ class Propagator:
         zs = np.linspace(0.0, self.length, total_steps + 1)
         storage_step = int(total_steps / traces)
         trace_z, trace_A = [], []
-        step = {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric,
-                "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced,
-                "ss_sym_midpoint": self.ss_sym_midpoint, "ss_agrawal": self.ss_agrawal}[method]
+        step = self.step_function(method)
         for i, z in enumerate(zs[:-1]):
             A = step(A, h)
             if traces != 1 and i % storage_step == 0:
@@ -583,8 +584,13 @@ class Propagator:
         h = self.length / traces if traces > total_steps else self.length / total_steps
         return 1e-6 if h > 1e-6 else h
 
+    def step_function(self, method):
+        return {"rk4ip": self.rk4ip, "ss_sym_rk4": self.ss_sym_rk4, "ss_symmetric": self.ss_symmetric,
+                "ss_simple": self.ss_simple, "ss_reduced": self.ss_reduced,
+                "ss_sym_midpoint": self.ss_sym_midpoint, "ss_agrawal": self.ss_agrawal}[method]
+
     def adaptive(self, A, local_error=1e-6, total_steps=100, traces=1, max_attempts=None,
-                 replay=None):
+                 replay=None, method="rk4ip"):
         """Step doubling with local extrapolation.
 
         ``max_attempts`` bounds the total number of attempts (a CPU-time cap used
@@ -595,7 +601,9 @@ class Propagator:
         h = self.initial_step(total_steps, traces)
         step_storage = self.length / traces
         z_ignore = step_storage
-        f_eta = np.power(2, self.ETA - 1.0)
+        step = self.step_function(method)
+        eta = self.ERRORS[method]  # stepper.py:143
+        f_eta = np.power(2, eta - 1.0)
         f_alpha = f_eta / (f_eta - 1.0)
         f_beta = 1.0 / (f_eta - 1.0)
         trace_z, trace_A, steps = [], [], []
@@ -605,9 +613,9 @@ class Propagator:
         attempts = rejected = 0
         if replay is not None:
             for h_acc in replay:
-                A_half = self.rk4ip(A, 0.5 * h_acc)
-                A_fine = self.rk4ip(A_half, 0.5 * h_acc)
-                A_coarse = self.rk4ip(A, h_acc)
+                A_half = step(A, 0.5 * h_acc)
+                A_fine = step(A_half, 0.5 * h_acc)
+                A_coarse = step(A, h_acc)
                 A = f_alpha * A_fine - f_beta * A_coarse
                 z += h_acc
                 steps.append((z, h_acc))
@@ -622,14 +630,14 @@ class Propagator:
                                    trace_z=trace_z, trace_A=trace_A, finished=False, h=h)
                 attempts += 1
                 h_half = 0.5 * h
-                A_half = self.rk4ip(A, h_half)
-                A_fine = self.rk4ip(A_half, h_half)
-                A_coarse = self.rk4ip(A, h)
+                A_half = step(A, h_half)
+                A_fine = step(A_half, h_half)
+                A_coarse = step(A, h)
                 delta = self.relative_local_error(A_fine, A_coarse)
                 h_temp = h
                 if delta > 0.0:
                     error_ratio = local_error / delta
-                    factor = self.SAFETY * np.power(error_ratio, 1.0 / self.ETA)
+                    factor = self.SAFETY * np.power(error_ratio, 1.0 / eta)
                     h = h_temp * min(self.MAX_FACTOR, max(self.MIN_FACTOR, factor))
                 else:
                     h = h_temp * self.MAX_FACTOR

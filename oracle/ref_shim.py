@@ -171,24 +171,35 @@ def make_fibre(**kwargs):
 
 
 class StepLog:
-    """Record every ``Solver.rk4ip`` call (z, h) made by a reference run."""
+    """Record every call (z, h) of one of the reference's step methods (``Solver.rk4ip``
+    by default; static or bound, solver.py:81)."""
 
-    def __init__(self):
+    def __init__(self, method="rk4ip"):
+        self.method = method
         self.calls = []
 
     def __enter__(self):
-        ref = load()
-        self._orig = ref.solver.Solver.rk4ip
+        cls = load().solver.Solver
+        self._raw = cls.__dict__[self.method]
         log = self.calls
-        orig = self._orig
+        if isinstance(self._raw, staticmethod):
+            orig = self._raw.__func__
 
-        def logged(A, z, h, f):
-            log.append((float(z), float(h)))
-            return orig(A, z, h, f)
+            def logged(A, z, h, f):
+                log.append((float(z), float(h)))
+                return orig(A, z, h, f)
 
-        ref.solver.Solver.rk4ip = staticmethod(logged)
+            setattr(cls, self.method, staticmethod(logged))
+        else:
+            orig = self._raw
+
+            def logged_bound(obj, A, z, h, f):
+                log.append((float(z), float(h)))
+                return orig(obj, A, z, h, f)
+
+            setattr(cls, self.method, logged_bound)
         return self
 
     def __exit__(self, *exc):
-        load().solver.Solver.rk4ip = staticmethod(self._orig)
+        setattr(load().solver.Solver, self.method, self._raw)
         return False

@@ -6,8 +6,10 @@ Run from the repository root in an environment that has the reference tree
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [case ...]
 
 Each case writes ``tests/golden/<case>.npz`` holding the seeded input field,
-the reference output field, the accepted (z, h) step sequence, the trace z
-values and peak powers, the FFT count and a JSON string with every parameter
+the reference output field, the accepted (z, h) step sequence, every call (z, h)
+of the step method (``rk4ip_calls``: Solver.rk4ip, or the split step of an adaptive
+split-step run), the trace z values and peak powers, the FFT count and a JSON string
+with every parameter
 needed to rebuild the run without the reference.  The tests compare the
 oracle restatement and the CUDA engine against these files; they never need
 the reference itself.
@@ -155,6 +157,20 @@ CASES = {
         fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
                    use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
                    method="ss_reduced", total_steps=800, traces=1)),
+    # Adaptive split steps (the stepper's leading-A methods with Solver.errors' orders,
+    # stepper.py:111-116,143): symmetric (order 3) and symmetric with RK4 (order 5).
+    "ass_symmetric_sc_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=False,
+                   use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
+                   method="ass_symmetric", local_error=1e-6, traces=1)),
+    "ass_sym_rk4_sc_1024": dict(
+        domain=dict(bit_width=12.5, samples_per_bit=1024, lambda_nm=835.0),
+        pulse=dict(kind="sech", peak_power=5.0e3, width=0.050, using_fwhm=True),
+        fibre=dict(length=5.0e-6, beta=BETA_SC, gamma=110.0, self_steepening=True,
+                   use_all="blowwood", f_R=0.18, tau_1=12.2e-3, tau_2=32.0e-3,
+                   method="ass_sym_rk4", local_error=1e-6, traces=1)),
     # Symmetric split step with the midpoint method on the nonlinear term
     # (solver.py:323-328): Raman + self-steepening supercontinuum and the N=2 soliton.
     "ss_sym_midpoint_sc_1024": dict(
@@ -205,13 +221,16 @@ def run_case(name, spec):
     ref = ref_shim.load()
     domain, dom_params = build_domain(ref, spec["domain"])
     A0 = build_input(ref, domain, spec["pulse"])
-    with ref_shim.StepLog() as log:
+    method = spec["fibre"]["method"].lower()
+    adaptive = method.startswith("a")
+    # the step method whose calls are logged: rk4ip, or the adaptive split step's method
+    logged = method[1:] if adaptive and method != "ark4ip" else "rk4ip"
+    with ref_shim.StepLog(logged) as log:
         fib = ref_shim.make_fibre(**spec["fibre"])
         t0 = time.time()
         A_out = fib(domain, A0.copy())
         wall = time.time() - t0
     st = fib.stepper.storage
-    adaptive = spec["fibre"]["method"].lower().startswith("a")
     steps = np.array(st.step_sizes if adaptive else [], float).reshape(-1, 2)
     calls = np.array(log.calls, float).reshape(-1, 2)
     trace_z = np.array(st.z, float)
@@ -225,7 +244,7 @@ def run_case(name, spec):
         out.update(yb_pump_out=np.float64(amp.Pp), yb_sigma12_s=np.asarray(amp.sigma12_s, float),
                    yb_sigma21_s=np.asarray(amp.sigma21_s, float))
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-    print(f"{name}: {wall:.2f} s, {len(calls)} rk4ip calls, fft {st.fft_total}, "
+    print(f"{name}: {wall:.2f} s, {len(calls)} step calls, fft {st.fft_total}, "
           f"peak_out {np.max(np.abs(A_out) ** 2):.6g}", flush=True)
 
 

@@ -25,8 +25,8 @@ def run_oracle(case):
     traces = fk.pop("traces", 1)
     tol = fk.pop("local_error", 1e-6)
     p = go.Propagator(grid, **fk)
-    if method == "ark4ip":
-        out, info = p.adaptive(case["A0"].copy(), tol, steps, traces)
+    if method.startswith("a"):  # the stepper's adaptive methods (stepper.py:111-116)
+        out, info = p.adaptive(case["A0"].copy(), tol, steps, traces, method=method[1:])
     else:
         out, info = p.standard(case["A0"].copy(), steps, traces, method=method)
     return p, out, info
