@@ -133,12 +133,16 @@ class Fibre:
                                       "the CUDA path")
         if use_Er_profile or use_Er_noise:
             raise NotImplementedError("the Er gain profile and ASE noise are not on the CUDA path")
-        if use_Yb_model and m.startswith("ss_"):
-            raise NotImplementedError("the split-step methods run without gain on the CUDA path")
         if small_signal_gain is not None and E_sat is None and P_sat is not None:
             if Tr is None:
                 raise Exception("Repetition rate is not defined.")
             E_sat = P_sat * Tr
+        gain = use_Yb_model or (small_signal_gain is not None and E_sat is not None)
+        if gain and m.startswith("ss_"):
+            raise NotImplementedError("the split-step methods run without gain on the CUDA path")
+        if self_steepening and m in ("ss_symmetric", "ss_simple", "ss_reduced"):
+            # the reference's exponential step divides by the field (nonlinearity.py:230-234)
+            raise NotImplementedError(f"{m} with self-steepening is not on the CUDA path")
         self.name = name
         self.length = length
         self.alpha, self.beta, self.gamma = alpha, beta, gamma

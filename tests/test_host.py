@@ -198,6 +198,11 @@ def test_fibre_model_options_on_the_cuda_path():
         Fibre(length=1e-3, gamma=5.0, use_Er_profile=True)
     with pytest.raises(NotImplementedError):
         Fibre(length=1e-3, gamma=5.0, method="ss_agrawal")
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, small_signal_gain=10.0, E_sat=1.0, method="ss_sym_rk4")
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, self_steepening=True, method="ss_reduced")
+    Fibre(length=1e-3, gamma=5.0, self_steepening=True, method="ss_sym_rk4")
 
 
 def test_engine_method_list_matches_the_plan():
