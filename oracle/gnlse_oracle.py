@@ -432,6 +432,40 @@ class MaximumStepsAllocatedError(StepperError):
     pass
 
 
+# ----------------------------------------------------------------------------
+# Explicit solvers and the fixed-step mesh on a generic ODE dA/dz = f(A, z)
+# ----------------------------------------------------------------------------
+def euler_step(A, z, h, f):
+    """``Solver.euler`` (solver.py:93-98)."""
+    k0 = h * f(A, z)
+    return A + k0
+
+
+def midpoint_step(A, z, h, f):
+    """``Solver.midpoint`` (solver.py:100-106)."""
+    k0 = h * f(A, z)
+    k1 = h * f(A + 0.5 * k0, z + 0.5 * h)
+    return A + k1
+
+
+def rk4_step(A, z, h, f):
+    """``Solver.rk4`` (solver.py:108-116)."""
+    k0 = h * f(A, z)
+    k1 = h * f(A + 0.5 * k0, z + 0.5 * h)
+    k2 = h * f(A + 0.5 * k1, z + 0.5 * h)
+    k3 = h * f(A + k2, z + h)
+    return A + (k0 + 2.0 * (k1 + k2) + k3) / 6.0
+
+
+def fixed_steps(step, A, f, length, total_steps):
+    """``Stepper.standard_stepper``'s mesh (stepper.py:164-201): h = length / steps and
+    z from ``linspace(0, length, steps + 1)``, one step from each z but the last."""
+    h = length / total_steps
+    for z in np.linspace(0.0, length, total_steps + 1)[:-1]:
+        A = step(A, z, h, f)
+    return A
+
+
 class Propagator:
     """RK4IP / ARK4IP propagation through one fibre, restated from the reference.
 
@@ -492,12 +526,8 @@ class Propagator:
 
     @staticmethod
     def rk4(A, h, f):
-        """``Solver.rk4`` (solver.py:109-116) for an autonomous f."""
-        k0 = h * f(A)
-        k1 = h * f(A + 0.5 * k0)
-        k2 = h * f(A + 0.5 * k1)
-        k3 = h * f(A + k2)
-        return A + (k0 + 2.0 * (k1 + k2) + k3) / 6.0
+        """``Solver.rk4`` (solver.py:109-116) for an autonomous f (``rk4_step``)."""
+        return rk4_step(A, 0.0, h, lambda x, z: f(x))
 
     def ss_symmetric(self, A, h):
         """``Solver.ss_symmetric`` (solver.py:267-275): linear half step, exponential
@@ -544,8 +574,7 @@ class Propagator:
         (solver.py:101-106) on the nonlinear term."""
         self.evals += 1
         A_L = self.linear(A, 0.5 * h)
-        k0 = h * self.n(A_L)
-        A_N = A_L + h * self.n(A_L + 0.5 * k0)
+        A_N = midpoint_step(A_L, 0.0, h, lambda x, z: self.n(x))
         return self.linear(A_N, 0.5 * h)
 
     def ss_sym_rk4(self, A, h):

@@ -127,3 +127,19 @@ def test_oracle_yb_cross_sections(name):
     s12, s21 = go.yb_cross_sections(grid, path)
     np.testing.assert_allclose(s12, case["yb_sigma12_s"], rtol=1e-13, atol=1e-40)
     np.testing.assert_allclose(s21, case["yb_sigma21_s"], rtol=1e-13, atol=1e-40)
+
+
+@pytest.mark.parametrize("step,steps,want", [
+    ("euler_step", 50, 0.72152686293820223), ("euler_step", 500, 0.71717199224362427),
+    ("midpoint_step", 50, 0.71663952968427402), ("midpoint_step", 500, 0.71669512731047913),
+    ("rk4_step", 50, 0.71669567757603803), ("rk4_step", 500, 0.71669567807363854)])
+def test_explicit_solvers_match_reference_golden_values(step, steps, want):
+    """pyofss/tests/test_solver.py:99-150 (CheckCoreRoutines): dA/dz = 3 exp(-4z) - 2A,
+    A(0) = 1, to z = 0.5 with the fixed-step stepper; the reference asserts these values
+    bit for bit, and so does this test (they pin the RK stage arithmetic and the z mesh
+    that the split steps ss_sym_rk4 / ss_sym_midpoint use)."""
+    def simple(A, z):
+        return 3.0 * np.exp(-4.0 * z) - 2.0 * A
+
+    got = go.fixed_steps(getattr(go, step), 1.0, simple, 0.5, steps)
+    assert got == want
