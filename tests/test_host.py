@@ -208,3 +208,19 @@ def test_fibre_model_options_on_the_cuda_path():
 def test_engine_method_list_matches_the_plan():
     from pyofsschanged_gb300.engine import METHODS
     assert gc.ENGINE_METHODS == set(METHODS)
+
+
+def test_large_grid_amplifier_tables_match_oracle():
+    """The 2^16-point amplifier configuration (100 ps at 1030 nm, saturable gain with a
+    40 nm Lorentzian, Raman and self-steepening): the host tables equal the oracle's."""
+    lam = 299792.458 / 1030.0
+    d = Domain(bit_width=100.0, samples_per_bit=65536, centre_nu=lam)
+    kw = dict(beta=[0.0, 0.0, 25.0, 0.05], gamma=5.0, self_steepening=True, use_all="blowwood",
+              small_signal_gain=39.09, E_sat=5.0, lamb0=1030.0, bandwidth=40.0)
+    g = GridTables(d, length=3e-3, **kw)
+    p = go.Propagator(go.Grid(bit_width=100.0, samples_per_bit=65536, centre_nu=lam), 3e-3, **kw)
+    np.testing.assert_allclose(g.beta_w, p.factor.imag, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(g.hR_re + 1j * g.hR_im, p.nl.h_R, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(g.ss_w, 1.0 + p.nl.omega * p.nl.ss_factor, rtol=1e-15)
+    np.testing.assert_allclose(g.gain_profile, p.gain.profile, rtol=1e-15)
+    assert g.gain_log == p.gain.gain_log and g.E_sat == p.gain.E_sat
