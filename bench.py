@@ -326,7 +326,8 @@ def run_ours(a):
     # spectral sums, the spectra stay on their ranks
     from pyofsschanged_gb300.ensemble import coherence_g12, coherence_g12_distributed, common_spectra
     spectra = common_spectra([x.cpu().numpy().astype(complex) for x in plan.unpack(work)])
-    g12 = coherence_g12_distributed(spectra) if world > 1 else coherence_g12(spectra)
+    g12 = (coherence_g12_distributed(spectra, n_bins=spectra.shape[1]) if world > 1
+           else coherence_g12(spectra))
     power = np.sum(np.abs(spectra) ** 2, axis=0)
     coherence = {"members": world * a.members,
                  "g12_power_weighted": float(np.sum(g12 * power) / np.sum(power))}

@@ -37,7 +37,11 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("PYOFSS_REFERENCE", "/root/reference")
+# The reference checkout: $PYOFSS_REFERENCE, else a directory named "reference" beside
+# this repository's root (the repository and the pyofss checkout side by side).
+REFERENCE_ROOT = os.environ.get(
+    "PYOFSS_REFERENCE",
+    os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference"))
 
 
 class _Stub(types.ModuleType):

@@ -54,7 +54,7 @@ static unsigned char* g_noalloc_dev[kMaxDevices];  // device address of g_noallo
 
 // FP32 tables from the FP64 staging copies of the caller's host arrays.
 __global__ void noalloc_tables(unsigned char* base, int n, double gamma, int has_ss, int raman,
-                               int gain, int has_profile) {
+                               int gain, int has_profile, int has_nu) {
   const double* stage = (const double*)(base + kStage);
   const double* ss = stage;
   const double* hre = stage + kNoAllocMaxN;
@@ -65,6 +65,7 @@ __global__ void noalloc_tables(unsigned char* base, int n, double gamma, int has
   float2* Hp = (float2*)(base + kHp);
   float2* tw = (float2*)(base + kTw);
   float2* twp = (float2*)(base + kTwp);
+  double* nu = (double*)(base + kNu);
   int logm = 0;
   while ((1 << logm) < n) ++logm;
   const int ntwp = gnlse::twp_size(logm, GNLSE_RADIX_BITS);
@@ -77,6 +78,9 @@ __global__ void noalloc_tables(unsigned char* base, int n, double gamma, int has
     Kr[a] = (float)(gamma * (has_ss ? ss[a] : 1.0));
     if (raman) Hp[a] = make_float2((float)(hre[a] / n), (float)(him[a] / n));
     if (gain) lor[a] = has_profile ? (float)gp[a] : 1.0f;
+    // without the caller's frequencies the photon number uses nu = 1, as the plan path
+    // does (the array may still hold an earlier call's table)
+    if (!has_nu) nu[a] = 1.0;
     double s, c;
     sincospi(2.0 * (double)a / (double)n, &s, &c);
     tw[a] = make_float2((float)c, (float)s);
@@ -135,7 +139,7 @@ extern "C" int gnlse_propagate_noalloc(const gnlse_grid_desc* gd, const gnlse_in
   if (e != cudaSuccess) return GNLSE_CUDA_ERROR;
   static_assert(gnlse::twp_size(12, GNLSE_RADIX_BITS) <= kTwpMax, "twiddle rows");
   noalloc_tables<<<(n + 255) / 256, 256, 0, s>>>(base, n, gd->gamma, gd->ss_w != nullptr, raman, gain,
-                                                  gd->gain_profile != nullptr);
+                                                  gd->gain_profile != nullptr, gd->nu != nullptr);
   if (cudaGetLastError() != cudaSuccess) return GNLSE_CUDA_ERROR;
 
   gnlse::GridDev g;

@@ -131,9 +131,16 @@ def shard(members, rank, world):
     return sorted(out[rank])
 
 
-def coherence_partial(spectra):
-    """Per-rank sums for coherence_g12: (sum_i A_i, sum_i |A_i|^2, count)."""
-    spectra = np.asarray(spectra)
+def coherence_partial(spectra, n_bins=None):
+    """Per-rank sums for coherence_g12: (sum_i A_i, sum_i |A_i|^2, count).
+
+    A rank whose shard is empty (more ranks than members) passes ``n_bins``, the
+    spectrum length, and contributes zero sums with count 0."""
+    spectra = np.asarray(spectra, dtype=complex)
+    if spectra.size == 0:
+        if n_bins is None:
+            raise ValueError("an empty shard needs n_bins (the spectrum length)")
+        return np.zeros(n_bins, complex), np.zeros(n_bins), 0
     return spectra.sum(axis=0), (np.abs(spectra) ** 2).sum(axis=0), spectra.shape[0]
 
 
@@ -145,12 +152,14 @@ def coherence_from_sums(s, p, n):
         return np.where(den > 0, num / den, 0.0)
 
 
-def coherence_g12_distributed(spectra, group=None):
+def coherence_g12_distributed(spectra, group=None, n_bins=None):
     """coherence_g12 over the union of every rank's spectra: one all-reduce of the
-    sums (torch.distributed, any backend), so the spectra themselves never move."""
+    sums (torch.distributed, any backend), so the spectra themselves never move.
+    Every rank passes ``n_bins`` (the common spectrum length) when some shard may be
+    empty."""
     import torch
     import torch.distributed as dist
-    s, p, n = coherence_partial(spectra)
+    s, p, n = coherence_partial(spectra, n_bins)
     dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
     buf = torch.tensor(np.concatenate([s.real, s.imag, p, [float(n)]]), dtype=torch.float64, device=dev)
     dist.all_reduce(buf, group=group)

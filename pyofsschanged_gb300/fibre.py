@@ -20,6 +20,8 @@ Models outside the CUDA path (WDM two-channel, the rs_factor term with self-stee
 the Er gain profile, ASE noise) raise ``NotImplementedError``.
 """
 
+import sys
+
 import numpy as np
 import torch
 
@@ -53,10 +55,31 @@ _STATUS_EXC = {
 }
 
 
+_BOTH = {}
+
+
+def stepper_exception(cls):
+    """The class to raise for one of the stepper exceptions above.
+
+    When pyofss's own stepper module (pyofss/modules/stepper.py:33-47) is loaded in
+    this process, a caller may catch pyofss's classes; the class returned then derives
+    from both this module's class and pyofss's class of the same name, so an
+    ``except`` clause written against either catches it.  Otherwise it is ``cls``.
+    """
+    ref = sys.modules.get("pyofss.modules.stepper")
+    rc = getattr(ref, cls.__name__, None) if ref is not None else None
+    if not (isinstance(rc, type) and issubclass(rc, Exception)) or issubclass(cls, rc):
+        return cls
+    key = (cls, rc)
+    if key not in _BOTH:
+        _BOTH[key] = type(cls.__name__, (cls, rc), {"__module__": __name__})
+    return _BOTH[key]
+
+
 def raise_for_status(status):
     if status in _STATUS_EXC:
         cls, msg = _STATUS_EXC[status]
-        raise cls(msg)
+        raise stepper_exception(cls)(msg)
     if status != nat.GNLSE_OK:
         raise nat.GnlseError(status, "propagation")
 
@@ -181,22 +204,27 @@ class Fibre:
         self.domain = domain
         st.storage(domain)
 
-    def __call__(self, domain, field):
-        if self.domain != domain or self._plan is None:
-            self._build(domain)
+    def _run(self, field):
+        """Propagate one field through the engine: (output field, stats, trace z values,
+        trace fields as a [k, n] device tensor)."""
         plan = self._plan
         flat = plan.pack([np.asarray(field)])
         plan.propagate(flat)
         stats = plan.stats()
         torch.cuda.current_stream(plan.device).synchronize()
-        st = stats[0]
+        z, As = plan.instance_traces(0, stats, device=True)
+        return plan.unpack(flat)[0].cpu().numpy().astype(complex), stats[0], z, As
+
+    def __call__(self, domain, field):
+        if self.domain != domain or self._plan is None:
+            self._build(domain)
+        out, st, z, As = self._run(field)
         self.stepper.stats = st
         if self.amplifier is not None:  # Amplifier2LevelModel.Pp after update_Pp calls
             self.amplifier.Pp = st["pump_w"]
         storage = self.stepper.storage
         storage.reset_array()
         storage.reset_characts()
-        z, As = plan.instance_traces(0, stats, device=True)
         storage.z = list(z)
         storage.As = [a.astype(complex) for a in As.cpu().numpy()]
         if len(z):
@@ -208,4 +236,4 @@ class Fibre:
             storage.step_sizes = []
         storage.fft_total = int(st["evals"]) * 16
         raise_for_status(st["status"])
-        return plan.unpack(flat)[0].cpu().numpy().astype(complex)
+        return out

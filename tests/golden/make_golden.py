@@ -1,7 +1,7 @@
 """Generate golden input/output vectors by running the unmodified pyofss reference.
 
 Run from the repository root in an environment that has the reference tree
-(``PYOFSS_REFERENCE``, default ``/root/reference``)::
+(``PYOFSS_REFERENCE``, default: a ``reference`` directory beside the repository root)::
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [case ...]
 

@@ -51,3 +51,29 @@ def test_coherence_allreduce_matches_single_process():
                            start_method="spawn")
         for r in range(world):
             np.testing.assert_allclose(out[r], ref, rtol=1e-12, atol=1e-15)
+
+
+def _rank_sharded(rank, world, port, spectra, out):
+    import torch.distributed as dist
+    from pyofsschanged_gb300.ensemble import coherence_g12_distributed
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mine = spectra[rank:rank + 1]  # ranks beyond the member count get an empty shard
+    out[rank] = coherence_g12_distributed(mine, n_bins=spectra.shape[1])
+    dist.destroy_process_group()
+
+
+def test_coherence_allreduce_with_empty_shards():
+    """More ranks than members: the ranks without members contribute zero sums and
+    every rank still gets the single-process |g12|."""
+    rng = np.random.default_rng(7)
+    spectra = rng.standard_normal((2, 32)) + 1j * rng.standard_normal((2, 32)) + 2.0
+    ref = coherence_g12(spectra)
+    world, port = 3, _free_port()
+    with mp.Manager() as mgr:
+        out = mgr.dict()
+        mp.start_processes(_rank_sharded, args=(world, port, spectra, out), nprocs=world, join=True,
+                           start_method="spawn")
+        for r in range(world):
+            np.testing.assert_allclose(out[r], ref, rtol=1e-12, atol=1e-15)

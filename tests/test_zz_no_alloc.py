@@ -103,3 +103,43 @@ def test_noalloc_rejects_yb_model(cuda_ready):
     rc = nat.lib().gnlse_propagate_noalloc(ct.byref(gd), ct.byref(idesc), ct.c_void_p(f.data_ptr()),
                                            None, ct.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == nat.GNLSE_UNSUPPORTED
+
+
+def test_noalloc_ignores_previous_call_tables(cuda_ready):
+    """A call that passes no Raman, self-steepening or frequency table must not use the
+    ones a previous call left in the shared array: the second call here has to match a
+    plan built from the same (absent) tables, and its photon numbers, taken with
+    nu = 1 as the plan path does, must be finite."""
+    case = gc.load("sc_blowwood_ark4ip_1024")
+    prm = case["params"]
+    d = Domain(**gc.domain_kwargs(prm))
+    fk = gc.fibre_kwargs(prm)
+    tol = fk.get("local_error", 1e-6)
+    full = GridTables(d, beta=fk["beta"], gamma=fk["gamma"], self_steepening=True,
+                      use_all="blowwood", length=fk["length"])
+    bare = GridTables(d, beta=fk["beta"], gamma=fk["gamma"], length=fk["length"])
+    bare.nu = None
+    assert full.hR_re is not None and full.ss_w is not None and bare.hR_re is None and bare.ss_w is None
+    inst = Instance(0, method="ark4ip", length=fk["length"], local_error=tol, traces=1)
+    plan = Plan([bare], [inst], precision="fp32")
+    ref = plan.pack([case["A0"]])
+    plan.propagate(ref)
+    want = ref.cpu().numpy().astype(complex)
+    st_want = plan.stats()[0]
+    lib = nat.lib()
+    stream = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for g, check in ((full, False), (bare, True)):
+        gd, idesc = descs(g, inst)
+        f = torch.as_tensor(case["A0"].astype(np.complex64)).cuda()
+        st = nat.Stats()
+        rc = lib.gnlse_propagate_noalloc(ct.byref(gd), ct.byref(idesc), ct.c_void_p(f.data_ptr()),
+                                         ct.byref(st), stream)
+        assert rc == nat.GNLSE_OK, nat.status_string(rc)
+        assert st.status == 0 and st.finished == 1
+        if check:
+            assert st.evals == st_want["evals"]
+            assert spec_err(f.cpu().numpy().astype(complex), want) <= TOL
+            for k in ("photons_in", "photons_out", "energy_in", "energy_out"):
+                v = getattr(st, k)
+                assert np.isfinite(v) and v > 0, (k, v)
+                assert abs(v - st_want[k]) <= 1e-5 * abs(st_want[k]), (k, v, st_want[k])
