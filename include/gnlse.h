@@ -80,8 +80,12 @@ enum {
  * GNLSE_FP64 complex128 throughout (fields complex128);
  * GNLSE_MIXED complex64 transforms and nonlinear evaluations with the
  * propagation state, RK accumulator and exp(hD) factors in double-float
- * (about 48 bits) and FP64 input/output transforms (fields complex128). */
-enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1, GNLSE_MIXED = 2 };
+ * (about 48 bits) and FP64 input/output transforms (fields complex128);
+ * GNLSE_DF double-float (about 48 bits, on FP32 instructions) throughout:
+ * transforms, nonlinear term, state and stage algebra, with the linear phase,
+ * error norm and step control in FP64 (fields complex128; grids of 1024 to
+ * 32768 points). */
+enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1, GNLSE_MIXED = 2, GNLSE_DF = 3 };
 
 /* One grid (pyofss Domain) with the fibre operators built on it. */
 typedef struct {

@@ -30,6 +30,7 @@ GNLSE_SS_REDUCED = 5
 GNLSE_FP32 = 0
 GNLSE_FP64 = 1
 GNLSE_MIXED = 2
+GNLSE_DF = 3
 
 _dp = ct.POINTER(ct.c_double)
 

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/gnlse.h"
@@ -84,9 +85,12 @@ bool supported(int precision, int logm, int C) {
 #define GNLSE_M32(R, L, CC) GNLSE_MATCH(GNLSE_FP32, R, L, CC)
 #define GNLSE_M64(R, L, CC) GNLSE_MATCH(GNLSE_FP64, R, L, CC)
 #define GNLSE_MMX(R, L, CC) GNLSE_MATCH(GNLSE_MIXED, R, L, CC)
+#define GNLSE_MDF(R, L, CC) GNLSE_MATCH(GNLSE_DF, R, L, CC)
   GNLSE_CLASSES_F32(GNLSE_M32)
   GNLSE_CLASSES_F64(GNLSE_M64)
   GNLSE_CLASSES_MIX(GNLSE_MMX)
+  GNLSE_CLASSES_DF(GNLSE_MDF)
+#undef GNLSE_MDF
 #undef GNLSE_M32
 #undef GNLSE_M64
 #undef GNLSE_MMX
@@ -100,9 +104,12 @@ cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, c
 #define GNLSE_C32(R, L, CC) GNLSE_CALL(GNLSE_FP32, false, R, L, CC)
 #define GNLSE_C64(R, L, CC) GNLSE_CALL(GNLSE_FP64, false, R, L, CC)
 #define GNLSE_CMX(R, L, CC) GNLSE_CALL(GNLSE_MIXED, true, R, L, CC)
+#define GNLSE_CDF(R, L, CC) GNLSE_CALL(GNLSE_DF, false, R, L, CC)
   GNLSE_CLASSES_F32(GNLSE_C32)
   GNLSE_CLASSES_F64(GNLSE_C64)
   GNLSE_CLASSES_MIX(GNLSE_CMX)
+  GNLSE_CLASSES_DF(GNLSE_CDF)
+#undef GNLSE_CDF
 #undef GNLSE_C32
 #undef GNLSE_C64
 #undef GNLSE_CMX
@@ -177,9 +184,12 @@ cudaError_t upload(gnlse_plan* p, const std::vector<T>& h, void** d) {
   return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// R: the transform element's real type (float, double or the double-float ddf);
+// extended: mixed-precision plans (FP64 boundary twiddles); want_cis: the
+// double-float cis(j pi / 512) table of the exp(hD) factors (mixed and df plans)
 template <class R>
 cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost& gh, GridDev& dv,
-                              bool extended) {
+                              bool extended, bool want_cis) {
   const int n = gd.n, C = gh.C, M = n / C;
   auto perm = [&](int a) { return (a % M) * C + a / M; };  // slot a = c*M + k2  <-  k = c + C*k2
   std::vector<double> beta(n), nu(n);
@@ -229,12 +239,13 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
     twl[2 * (size_t)j + 1] = tw[2 * (size_t)j * C + 1];
   }
   // per-pass twiddle rows of the M-point transform
-  const int logm = gh.logm, ntwp = twp_size(logm, GNLSE_RADIX_BITS);
+  const int rb = std::is_same<R, ddf>::value ? GNLSE_DF_RADIX_BITS : GNLSE_RADIX_BITS;  // the engine's radix
+  const int logm = gh.logm, ntwp = twp_size(logm, rb);
   std::vector<R> twp(2 * (size_t)ntwp);
   std::vector<double> twp64(extended ? 2 * (size_t)ntwp : 0);
   for (int e2 = 0; e2 < ntwp; ++e2) {
     const long double ang = 2.0L * 3.14159265358979323846264338327950288L *
-                            (long double)twp_exponent(logm, GNLSE_RADIX_BITS, e2) / (long double)M;
+                            (long double)twp_exponent(logm, rb, e2) / (long double)M;
     const double c = (double)cosl(ang), sn = (double)sinl(ang);
     twp[2 * (size_t)e2] = (R)c;
     twp[2 * (size_t)e2 + 1] = (R)sn;
@@ -246,21 +257,11 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
   cudaError_t e;
   if ((e = upload(p, twp, &gh.d_twp)) != cudaSuccess) return e;
   if (extended && (e = upload(p, twp64, &gh.d_twp64)) != cudaSuccess) return e;
-  if (extended) {
-    // FP64 twiddles for the boundary transforms and the double-float
-    // cis(j pi/512) table of the exp(hD) factors
-    std::vector<double> tw64(2 * (size_t)n), twl64(2 * (size_t)M);
+  const long double PI_L = 3.14159265358979323846264338327950288L;
+  if (want_cis) {
+    // double-float cis(j pi/512), j < 1024, of the exp(hD) factors: float4
+    // {cos hi, sin hi, cos lo, sin lo}
     std::vector<float> cis(4 * 1024);
-    const long double PI_L = 3.14159265358979323846264338327950288L;
-    for (int j = 0; j < n; ++j) {
-      const long double ang = 2.0L * PI_L * (long double)j / (long double)n;
-      tw64[2 * (size_t)j] = (double)std::cos((double)ang);
-      tw64[2 * (size_t)j + 1] = (double)std::sin((double)ang);
-    }
-    for (int j = 0; j < M; ++j) {
-      twl64[2 * (size_t)j] = tw64[2 * (size_t)j * C];
-      twl64[2 * (size_t)j + 1] = tw64[2 * (size_t)j * C + 1];
-    }
     for (int j = 0; j < 1024; ++j) {
       const long double ang = PI_L * (long double)j / 512.0L;
       const long double c = cosl(ang), sn = sinl(ang);
@@ -270,9 +271,22 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
       cis[4 * j + 2] = (float)(c - (long double)ch);
       cis[4 * j + 3] = (float)(sn - (long double)sh);
     }
+    if ((e = upload(p, cis, &gh.d_cis)) != cudaSuccess) return e;
+  }
+  if (extended) {
+    // FP64 twiddles for the boundary transforms
+    std::vector<double> tw64(2 * (size_t)n), twl64(2 * (size_t)M);
+    for (int j = 0; j < n; ++j) {
+      const long double ang = 2.0L * PI_L * (long double)j / (long double)n;
+      tw64[2 * (size_t)j] = (double)std::cos((double)ang);
+      tw64[2 * (size_t)j + 1] = (double)std::sin((double)ang);
+    }
+    for (int j = 0; j < M; ++j) {
+      twl64[2 * (size_t)j] = tw64[2 * (size_t)j * C];
+      twl64[2 * (size_t)j + 1] = tw64[2 * (size_t)j * C + 1];
+    }
     if ((e = upload(p, tw64, &gh.d_tw64)) != cudaSuccess) return e;
     if ((e = upload(p, twl64, &gh.d_twl64)) != cudaSuccess) return e;
-    if ((e = upload(p, cis, &gh.d_cis)) != cudaSuccess) return e;
   }
   if ((e = upload(p, twl, &gh.d_twl)) != cudaSuccess) return e;
   if ((e = upload(p, beta, &gh.d_beta)) != cudaSuccess) return e;
@@ -358,7 +372,8 @@ int gnlse_class_supported(int precision, int log2_points_per_cta, int cluster) {
 }
 
 int gnlse_set_class_cost(int precision, int log2_points_per_cta, int cluster, double sm_us) {
-  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED) return GNLSE_BAD_ARGUMENT;
+  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED && precision != GNLSE_DF)
+    return GNLSE_BAD_ARGUMENT;
   if (!supported(precision, log2_points_per_cta, cluster)) return GNLSE_UNSUPPORTED;
   std::lock_guard<std::mutex> lk(g_cost_mu);
   for (size_t k = 0; k < g_cost.size(); ++k) {
@@ -376,7 +391,7 @@ int gnlse_set_class_cost(int precision, int log2_points_per_cta, int cluster, do
 int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, int n_instances,
                       const gnlse_instance_desc* instances, gnlse_plan** plan_out) {
   if (!plan_out || !grids || !instances || n_grids <= 0 || n_instances <= 0) return GNLSE_BAD_ARGUMENT;
-  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED)
+  if (precision != GNLSE_FP32 && precision != GNLSE_FP64 && precision != GNLSE_MIXED && precision != GNLSE_DF)
     return GNLSE_BAD_ARGUMENT;
   *plan_out = nullptr;
   gnlse_plan* p = new (std::nothrow) gnlse_plan();
@@ -407,8 +422,8 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       tput[i] = lat[i] = C;
       continue;
     }
-    if (precision == GNLSE_FP64 && !tuned(precision)) {
-      // complex128: 4096 points per CTA (one CTA per SM), larger grids span a cluster
+    if ((precision == GNLSE_FP64 || precision == GNLSE_DF) && !tuned(precision)) {
+      // 16-byte elements: 4096 points per CTA, larger grids span a cluster
       const int C = n <= 4096 ? 1 : n / 4096;
       if (C > 8 || !supported(precision, ilog2i(n / C), C)) {
         free_plan(p);
@@ -552,8 +567,11 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     gh.C = vC[v];
     gh.logm = ilog2i(gd.n / gh.C);
     cudaError_t e = precision == GNLSE_FP64
-                        ? build_grid_tables<double>(p, gd, gh, gdev[v], false)
-                        : build_grid_tables<float>(p, gd, gh, gdev[v], precision == GNLSE_MIXED);
+                        ? build_grid_tables<double>(p, gd, gh, gdev[v], false, false)
+                        : precision == GNLSE_DF
+                              ? build_grid_tables<ddf>(p, gd, gh, gdev[v], false, true)
+                              : build_grid_tables<float>(p, gd, gh, gdev[v], precision == GNLSE_MIXED,
+                                                         precision == GNLSE_MIXED);
     if (e != cudaSuccess) {
       free_plan(p);
       return cuda_fail(e);

@@ -24,6 +24,7 @@
 
 #include <type_traits>
 
+#include "gnlse_dd.cuh"
 #include "gnlse_df.cuh"
 #include "gnlse_twiddle.h"
 #include "gnlse_types.h"
@@ -67,6 +68,21 @@ namespace gnlse {
 template <class R> struct VT;
 template <> struct VT<float> { using V = float2; };
 template <> struct VT<double> { using V = double2; };
+template <> struct VT<ddf> { using V = ddc; };  // double-float transforms ("df" plans)
+
+// Read-only (non-coherent cache) load of a table entry of any element type.
+template <class T>
+__device__ __forceinline__ T ldro(const T* p) {
+  if constexpr (std::is_same<T, ddf>::value) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return ddf(v.x, v.y);
+  } else if constexpr (std::is_same<T, ddc>::value) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return ddc{ddf(v.x, v.y), ddf(v.z, v.w)};
+  } else {
+    return __ldg(p);
+  }
+}
 
 template <class V> __device__ __forceinline__ V mk(decltype(V::x) a, decltype(V::x) b) { V r; r.x = a; r.y = b; return r; }
 template <class V> __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
@@ -145,7 +161,7 @@ __device__ __forceinline__ void dft(V (&v)[RAD]) {
           v[blk + j + half] = SIGN > 0 ? mk<V>(-d.y, d.x) : mk<V>(d.y, -d.x);
         } else {
           const S c = (S)c16(m), s = (S)(SIGN * s16(m));
-          v[blk + j + half] = mk<V>(d.x * c - d.y * s, d.x * s + d.y * c);
+          v[blk + j + half] = cmul(d, mk<V>(c, s));  // d.x c - d.y s + i (d.x s + d.y c)
         }
       }
     }
@@ -176,14 +192,17 @@ __device__ __forceinline__ double simpson_w(int n, int N) {
 template <class R, int LOGM, int C, bool XS = false, bool INPLACE = false>
 struct Engine {
   using V = typename VT<R>::V;
+  // DD: double-float transforms, nonlinear term and state (complex128 user fields)
+  static constexpr bool DD = std::is_same<R, ddf>::value;
   using SV = typename std::conditional<XS, float4, V>::type;  // state-like arrays
-  using FV = typename std::conditional<XS, double2, V>::type;  // user fields / traces
+  using FV = typename std::conditional<XS || DD, double2, V>::type;  // user fields / traces
   static_assert(!XS || sizeof(R) == 4, "extended state runs on complex64 transforms");
   static constexpr int M = 1 << LOGM;
   static constexpr int N = M * C;
-  static constexpr int T = (M / GNLSE_PPT) < GNLSE_TMIN ? GNLSE_TMIN : (M / GNLSE_PPT);
+  static constexpr int RB = DD ? GNLSE_DF_RADIX_BITS : GNLSE_RADIX_BITS;  // log2 of the main radix
+  static constexpr int PPT = DD ? (1 << GNLSE_DF_RADIX_BITS) : GNLSE_PPT;   // points per thread per pass
+  static constexpr int T = (M / PPT) < GNLSE_TMIN ? GNLSE_TMIN : (M / PPT);
   static constexpr int MP = M + M / 16;
-  static constexpr int RB = GNLSE_RADIX_BITS;  // log2 of the main radix (gnlse_twiddle.h)
   static constexpr int RADIX = 1 << RB;
   static constexpr int NR16 = LOGM / RB;        // passes of the main radix
   static constexpr int REM = LOGM % RB;         // log2 of the final smaller radix
@@ -622,8 +641,8 @@ struct Engine {
   // gain exponent of one linear-operator call: ga lor (saturable amplifier), or
   // ga alpha_s N + gb eta_s (Yb model; ga = 500 h n2, gb = -500 h)
   static __device__ __forceinline__ R gexp(const Op& op, int a, R ga) {
-    R x = ga * __ldg(&op.lor[a]);
-    if (op.gain == 2) x = fma(op.gb, __ldg(&op.lor2[a]), x);
+    R x = ga * ldro(&op.lor[a]);
+    if (op.gain == 2) x = fma(op.gb, ldro(&op.lor2[a]), x);
     return x;
   }
   static __device__ __forceinline__ V mult(const Op& op, int a, V e, R ga) {
@@ -684,7 +703,7 @@ struct Engine {
       auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
       auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
       fwd(cx, P, rdPt, wrP, false, false);
-      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
+      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], ldro(&Hp[o * M + l])); };
       auto e3 = [&](int n1, int n2, V conv) {
         const int s = pad(tslot(n1, n2));
         V x = X[s];
@@ -739,6 +758,22 @@ struct Engine {
     return c;
   }
 
+  // user field element <-> transform element (double-float plans convert complex128)
+  static __device__ __forceinline__ V fv2v(const FV& f) {
+    if constexpr (DD) {
+      return V{R(f.x), R(f.y)};
+    } else {
+      return f;
+    }
+  }
+  static __device__ __forceinline__ FV v2fv(const V& v) {
+    if constexpr (DD) {
+      return make_double2((double)v.x, (double)v.y);
+    } else {
+      return v;
+    }
+  }
+
   // time -> spectral state: S = G+(field)
   static __device__ __noinline__ void to_spectral(const Ctx& cx, const GridDev& g, const FV* field, SV* S) {
     if constexpr (XS) {
@@ -749,7 +784,7 @@ struct Engine {
       };
       E64::fwd(c, c.X, pro, epi);
     } else {
-      auto pro = [&](int o, int l) -> V { return field[o * M + l]; };
+      auto pro = [&](int o, int l) -> V { return fv2v(field[o * M + l]); };
       auto epi = [&](int o, int l, V v) { S[o * M + l] = v; };
       fwd(cx, cx.P, pro, epi);
     }
@@ -769,7 +804,7 @@ struct Engine {
     } else {
       const R invN = (R)(1.0 / (double)N);
       auto pro = [&](int o, int l) -> V { return S[o * M + l]; };
-      auto epi = [&](int o, int l, V v) { field[o * M + l] = cscale(v, invN); };
+      auto epi = [&](int o, int l, V v) { field[o * M + l] = v2fv(cscale(v, invN)); };
       inv(cx, cx.P, pro, epi);
     }
   }
@@ -785,7 +820,7 @@ struct Engine {
     // the attenuation factor is 1 for a lossless fibre (skips an FP64 exp per thread)
     const double mag = g.alpha != 0.0 ? exp(-0.5 * g.alpha * hh) : 1.0;
     const int base = cx.rank * M;
-    if constexpr (XS) {
+    if constexpr (XS || DD) {
       const float4* tab = (const float4*)g.cis_df;
       const dff magd = df_from_double(mag);
       const bool lossy = g.alpha != 0.0;
@@ -808,8 +843,16 @@ struct Engine {
         const float4 tv = __ldg(&tab[ji]);
         dfc e = dfc_mul(dfc{{tv.x, tv.z}, {tv.y, tv.w}}, dfc{cs, sn});
         if (lossy) e = dfc_scale(e, magd);
-        dfc_store(E1, a, e);
-        if (E2) dfc_store(E2, a, dfc_mul(e, e));
+        if constexpr (XS) {
+          dfc_store(E1, a, e);
+          if (E2) dfc_store(E2, a, dfc_mul(e, e));
+        } else {
+          E1[a] = V{ddf(e.re.hi, e.re.lo), ddf(e.im.hi, e.im.lo)};
+          if (E2) {
+            const dfc e2 = dfc_mul(e, e);
+            E2[a] = V{ddf(e2.re.hi, e2.re.lo), ddf(e2.im.hi, e2.im.lo)};
+          }
+        }
       }
     } else {
       for (int l = threadIdx.x; l < M; l += T) {
@@ -929,7 +972,7 @@ struct Engine {
     const int base = cx.rank * M;
     V* X = cx.X;
     struct In { V x; R k; };
-    each_slot<4, In>([&](int l) { return In{X[pad(l)], __ldg(&Kr[base + l])}; },
+    each_slot<4, In>([&](int l) { return In{X[pad(l)], ldro(&Kr[base + l])}; },
                      [&](int l, const In& r) { MA[base + l] = ik(r.k, r.x); });
     __syncthreads();
   }
@@ -965,7 +1008,7 @@ struct Engine {
     each_slot<4, In>(
         [&](int l) {
           const int a = base + l;
-          return In{X[pad(l)], __ldg(&op.Kr[a]), lds(op.Et, a), lds(op.S0, a), op.MA0[a]};
+          return In{X[pad(l)], ldro(&op.Kr[a]), lds(op.Et, a), lds(op.S0, a), op.MA0[a]};
         },
         [&](int l, const In& r) {
           const int a = base + l;
@@ -995,7 +1038,7 @@ struct Engine {
     each_slot<4, In>(
         [&](int l) {
           const int a = base + l;
-          return In{X[pad(l)], __ldg(&op.Kr[a]), lds(op.acc, a), ldv(op.Et, a), ldv(op.S0, a)};
+          return In{X[pad(l)], ldro(&op.Kr[a]), lds(op.acc, a), ldv(op.Et, a), ldv(op.S0, a)};
         },
         [&](int l, const In& r) {
           const int a = base + l;
@@ -1059,7 +1102,7 @@ struct Engine {
       auto rdPt = [&](int n1, int n2) -> V { return P[pad(tslot(n1, n2))]; };
       auto wrP = [&](int, int l, V v) { P[pad(l)] = v; };
       fwd(cx, P, rdPt, wrP);
-      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], __ldg(&Hp[o * M + l])); };
+      auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], ldro(&Hp[o * M + l])); };
       auto e3 = [&](int n1, int n2, V conv) {
         const int sl = pad(tslot(n1, n2));
         P[sl] = mk<V>(f1 * cabs2(X[sl]) + fR * conv.x, fR * conv.y);
@@ -1068,20 +1111,28 @@ struct Engine {
     }
     __syncthreads();
     // Delta = (exp(i gamma h t) - 1) B in X: exp(x + iy) - 1 = expm1(x) cos y - 2 sin^2(y/2) + i e^x sin y
-    const double gh = h * (double)__ldg((const R*)g.Kr);  // gamma h (Kr = gamma without self-steepening)
+    const double gh = h * (double)ldro((const R*)g.Kr);  // gamma h (Kr = gamma without self-steepening)
     for (int l = threadIdx.x; l < M; l += T) {
       const V t = P[pad(l)];
       const V b = Bt[tsample(cx.rank, l)];
       const R px = (R)(-gh) * t.y, py = (R)gh * t.x;
-      R sn, cs;
-      if constexpr (sizeof(R) == 4) {
-        sincosf(py, &sn, &cs);
+      V ephi;
+      if constexpr (DD) {  // the phase factor in FP64, ~1e-16, rounded to double-float
+        double sn, cs;
+        sincos((double)py, &sn, &cs);
+        const double hs = sin(0.5 * (double)py), em1 = expm1((double)px);
+        ephi = mk<V>(R(em1 * cs - 2.0 * hs * hs), R((em1 + 1.0) * sn));
       } else {
-        sincos(py, &sn, &cs);
+        R sn, cs;
+        if constexpr (sizeof(R) == 4) {
+          sincosf(py, &sn, &cs);
+        } else {
+          sincos(py, &sn, &cs);
+        }
+        const R hs = sizeof(R) == 4 ? sinf(0.5f * (float)py) : (R)sin(0.5 * (double)py);
+        const R em1 = sizeof(R) == 4 ? expm1f((float)px) : (R)expm1((double)px);
+        ephi = mk<V>(em1 * cs - (R)2 * hs * hs, (em1 + (R)1) * sn);
       }
-      const R hs = sizeof(R) == 4 ? sinf(0.5f * (float)py) : (R)sin(0.5 * (double)py);
-      const R em1 = sizeof(R) == 4 ? expm1f((float)px) : (R)expm1((double)px);
-      const V ephi = mk<V>(em1 * cs - (R)2 * hs * hs, (em1 + (R)1) * sn);
       X[pad(l)] = cmul(ephi, b);
     }
     __syncthreads();
@@ -1139,7 +1190,7 @@ struct Engine {
           const int a = base + l;
           In r;
           r.x = X[pad(l)];
-          r.k = __ldg(&op.Kr[a]);
+          r.k = ldro(&op.Kr[a]);
           r.e = lds(op.Et, a);
           r.acc = lds(op.acc, a);
           if (coarse) r.sf = lds(op.Sf, a);
@@ -1176,8 +1227,8 @@ struct Engine {
             }
           }
         });
-    s[0] = d2;
-    s[1] = f2;
+    s[0] = (double)d2;
+    s[1] = (double)f2;
     s[2] = bad;
     if (coarse) {
       cluster_sum<3>(cx, s);

@@ -1,0 +1,3 @@
+// Kernel instantiation: double-float, M = 2^11 points per CTA, cluster of 2.
+#include "gnlse_inst.inc"
+GNLSE_INSTANTIATE(gnlse::ddf, 11, 2)

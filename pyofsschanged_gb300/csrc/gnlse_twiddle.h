@@ -11,6 +11,11 @@
 #ifndef GNLSE_RADIX_BITS
 #define GNLSE_RADIX_BITS 4
 #endif
+// double-float plans: radix-8 passes, 8 points per thread (a radix-16 butterfly of
+// 16-byte double-float values needs the whole register file of a 256-thread CTA)
+#ifndef GNLSE_DF_RADIX_BITS
+#define GNLSE_DF_RADIX_BITS 3
+#endif
 
 #if defined(__CUDACC__)
 #define GNLSE_HD __host__ __device__

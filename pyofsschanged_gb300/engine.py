@@ -3,8 +3,9 @@
 A :class:`Plan` owns the device operator tables, per-instance state and
 scratch of the C engine (include/gnlse.h).  Fields are torch tensors on the
 current CUDA device: complex64 for ``precision="fp32"``, complex128 for
-``"fp64"`` and ``"mixed"`` (complex64 transforms with a double-float state),
-concatenated per instance in the order given.
+``"fp64"``, ``"mixed"`` (complex64 transforms with a double-float state) and
+``"df"`` (double-float transforms, nonlinear term and state), concatenated per
+instance in the order given.
 """
 
 import ctypes as ct
@@ -14,7 +15,8 @@ import torch
 
 from . import _native as nat
 
-PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE_MIXED}
+PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE_MIXED,
+              "df": nat.GNLSE_DF}
 METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP, "ss_sym_rk4": nat.GNLSE_SS_SYM_RK4,
            "ss_symmetric": nat.GNLSE_SS_SYMMETRIC, "ss_simple": nat.GNLSE_SS_SIMPLE,
            "ss_reduced": nat.GNLSE_SS_REDUCED}
@@ -55,7 +57,7 @@ class Instance:
 class Plan:
     def __init__(self, grids, instances, precision="fp32", device=None):
         if precision not in PRECISIONS:
-            raise ValueError("precision must be 'fp32', 'mixed' or 'fp64'")
+            raise ValueError("precision must be 'fp32', 'mixed', 'df' or 'fp64'")
         lib = nat.lib()
         self.precision = precision
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
