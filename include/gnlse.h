@@ -89,8 +89,9 @@ enum { GNLSE_FP32 = 0, GNLSE_FP64 = 1, GNLSE_MIXED = 2, GNLSE_DF = 3 };
 
 /* One grid (pyofss Domain) with the fibre operators built on it. */
 typedef struct {
-  int32_t n;                  /* samples: power of two, 256 .. 65536 (FP64: .. 32768) */
-  int32_t cluster;            /* CTAs per field: 0 = automatic, else 1, 2, 4 or 8 */
+  int32_t n;                  /* samples: power of two, 256 .. 65536 (GNLSE_DF: 1024 ..) */
+  int32_t cluster;            /* CTAs per field: 0 = automatic, else 1, 2, 4, 8 or 16 (a
+                                 non-portable cluster: 65536-point fp64 / df grids) */
   double dt;                  /* Domain.dt, ps */
   double window_t;            /* Domain.window_t, ps */
   const double* beta_w;       /* [n] fftshift(sum_k beta_k (w - w0)^k / k!), 1/km */

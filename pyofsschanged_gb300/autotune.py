@@ -28,7 +28,7 @@ def candidates(n, precision):
     p = PRECISIONS[precision]
     mcap = 8192 if n > 8 * 4096 else 4096
     out = []
-    for c in (1, 2, 4, 8):
+    for c in (1, 2, 4, 8, 16):
         m = n // c
         if m < 256 or m > mcap or m * c != n:
             continue
@@ -102,6 +102,36 @@ def clear(precision="mixed"):
     lib = nat.lib()
     p = PRECISIONS[precision]
     for logm in range(8, 14):
-        for c in (1, 2, 4, 8):
+        for c in (1, 2, 4, 8, 16):
             if lib.gnlse_class_supported(p, logm, c):
                 lib.gnlse_set_class_cost(p, logm, c, 0.0)
+
+
+def main(argv=None):
+    """One saturated measurement of one launch class on the benchmark ensemble's grid:
+
+        python -m pyofsschanged_gb300.autotune --precision df --n 16384 --cluster 8
+
+    runs a warm-up launch (2 attempts per member) and the timed launch (``--attempts``
+    per member) of ``--ctas`` CTAs per SM, and prints the SM time per attempt; the timed
+    launch is the one a profiler capture of that class records (its second launch)."""
+    import argparse
+
+    from .ensemble import ensemble_plan_inputs, sc_ensemble
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--precision", default="df", choices=sorted(PRECISIONS))
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--cluster", type=int, default=8)
+    ap.add_argument("--attempts", type=int, default=4)
+    ap.add_argument("--ctas", type=int, default=32)
+    a = ap.parse_args(argv)
+    members, domains, fields = sc_ensemble(256)
+    idx = [i for i, m in enumerate(members) if m.n == a.n][:8]
+    grids, _ = ensemble_plan_inputs([members[i] for i in idx], {a.n: domains[a.n]})
+    us = measure(grids[0], [fields[i] for i in idx], a.cluster, a.precision, a.attempts, a.ctas)
+    print(json.dumps({"precision": a.precision, "n": a.n, "cluster": a.cluster,
+                      "attempts_per_member": a.attempts, "sm_us_per_attempt": us}))
+
+
+if __name__ == "__main__":
+    main()

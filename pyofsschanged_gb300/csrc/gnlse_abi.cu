@@ -415,7 +415,8 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     }
     if (gd.cluster != 0) {
       const int C = gd.cluster;
-      if ((C != 1 && C != 2 && C != 4 && C != 8) || n % C != 0 || !supported(precision, ilog2i(n / C), C)) {
+      if ((C != 1 && C != 2 && C != 4 && C != 8 && C != 16) || n % C != 0 ||
+          !supported(precision, ilog2i(n / C), C)) {
         free_plan(p);
         return GNLSE_UNSUPPORTED;
       }
@@ -425,7 +426,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     if ((precision == GNLSE_FP64 || precision == GNLSE_DF) && !tuned(precision)) {
       // 16-byte elements: 4096 points per CTA, larger grids span a cluster
       const int C = n <= 4096 ? 1 : n / 4096;
-      if (C > 8 || !supported(precision, ilog2i(n / C), C)) {
+      if (C > 16 || !supported(precision, ilog2i(n / C), C)) {
         free_plan(p);
         return GNLSE_UNSUPPORTED;
       }
@@ -439,7 +440,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     // except for grids above 8 x 4096 points.
     const int mcap = n > 8 * 4096 ? 13 : 12;
     int best = 0, fast = 0;
-    for (int C = 1; C <= 8; C *= 2) {
+    for (int C = 1; C <= 16; C *= 2) {
       const int logm = ilog2i(n / C);
       if (n / C < 256 || logm > mcap || !supported(precision, logm, C)) continue;
       if (!best || sm_cost(precision, logm, C) < sm_cost(precision, ilog2i(n / best), best)) best = C;
@@ -449,7 +450,7 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
       return GNLSE_UNSUPPORTED;
     }
     const double cb = sm_cost(precision, ilog2i(n / best), best);
-    for (int C = 1; C <= 8; C *= 2) {
+    for (int C = 1; C <= 16; C *= 2) {
       const int logm = ilog2i(n / C);
       if (n / C < 256 || logm > mcap || !supported(precision, logm, C) || sm_cost(precision, logm, C) > 1.5 * cb) continue;
       if (!fast || sm_cost(precision, logm, C) / C < sm_cost(precision, ilog2i(n / fast), fast) / fast) fast = C;

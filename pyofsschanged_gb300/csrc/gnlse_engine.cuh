@@ -208,7 +208,7 @@ struct Engine {
   static constexpr int REM = LOGM % RB;         // log2 of the final smaller radix
   static constexpr int RED = 64;  // doubles of reduction scratch
   static_assert(LOGM >= 8, "M >= 256 required");
-  static_assert(C == 1 || C == 2 || C == 4 || C == 8, "cluster size 1, 2, 4 or 8");
+  static_assert(C == 1 || C == 2 || C == 4 || C == 8 || C == 16, "cluster size 1, 2, 4, 8 or 16");
   static constexpr size_t ctl_bytes() { return 1024; }
   // CTAs that fit on one SM by shared memory (228 KB per SM, 1 KB reserved per CTA)
   static constexpr int NBUF = (C > 1 && !INPLACE) ? 3 : 2;  // X, P (+ W)
@@ -1646,6 +1646,10 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
   cudaError_t err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C, XS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
+  if (C > 8) {  // 16-CTA clusters are beyond the portable limit of 8
+    err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C, XS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (err != cudaSuccess) return err;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_clusters * C);
   cfg.blockDim = dim3(E::T);

@@ -32,11 +32,11 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
 #define GNLSE_CLASSES_F64(X) \
   X(double, 8, 1) X(double, 9, 1) X(double, 10, 1) X(double, 11, 1) X(double, 12, 1) \
   X(double, 8, 2) X(double, 9, 2) X(double, 10, 2) X(double, 11, 2) X(double, 12, 2) \
-  X(double, 8, 4) X(double, 12, 4) X(double, 12, 8)
+  X(double, 8, 4) X(double, 12, 4) X(double, 12, 8) X(double, 12, 16)
 // double-float classes: ~48-bit transforms, nonlinear term and state on FP32 instructions
 #define GNLSE_CLASSES_DF(X) \
   X(ddf, 10, 1) X(ddf, 11, 1) X(ddf, 12, 1) X(ddf, 11, 2) X(ddf, 12, 2) \
-  X(ddf, 11, 4) X(ddf, 12, 4) X(ddf, 11, 8) X(ddf, 12, 8)
+  X(ddf, 11, 4) X(ddf, 12, 4) X(ddf, 11, 8) X(ddf, 12, 8) X(ddf, 12, 16)
 // extended-state (mixed precision) classes: complex64 transforms
 #define GNLSE_CLASSES_MIX(X) \
   X(float, 8, 1) X(float, 9, 1) X(float, 10, 1) X(float, 11, 1) X(float, 12, 1) \

@@ -62,3 +62,13 @@ def energy(a_t, t):
     """Pulse energy in nJ (Simpson rule over t in ps, power in W)."""
     dt = t[1] - t[0]
     return float(np.sum(simpson_weights(len(a_t)) * np.abs(a_t) ** 2) * dt * 1e-3)
+
+
+def spectral_phase(a_t, domain, gdd, centre_omega=None):
+    """The field with the quadratic spectral phase exp(i gdd/2 (w - w0)^2) applied: a
+    linear chirp of group-delay dispersion ``gdd`` (ps^2), the phase propagation through
+    a length z of a fibre with beta_2 z = gdd acquires in the dispersion operator
+    i sum_n beta_n (w - w0)^n / n! (pyofss/modules/linearity.py:162-186)."""
+    w0 = domain.centre_omega if centre_omega is None else centre_omega
+    dw = fftshift(np.asarray(domain.omega) - w0)
+    return ifft(np.exp(0.5j * gdd * dw * dw) * fft(np.asarray(a_t, complex)))
