@@ -27,6 +27,7 @@ struct ClassRun {
   int first;  // offset into the order array
   int count;
   int level;  // 0 = longest predicted propagations (highest stream priority)
+  int kinds;  // kernels its instances need: 1 RK4IP stage loop, 2 exponential split steps
 };
 
 // SM time (us) of one attempt of one field in class (logm, C), measured on
@@ -98,9 +99,10 @@ bool supported(int precision, int logm, int C) {
   return false;
 }
 
-cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, cudaStream_t s) {
-#define GNLSE_CALL(PREC, XS, R, L, CC) \
-  if (precision == (PREC) && logm == (L) && C == (CC)) return launch_class<R, L, CC, XS>(kp, n, s);
+cudaError_t dispatch1(int precision, int logm, int C, const KParams& kp, int n, cudaStream_t s, int kind) {
+#define GNLSE_CALL(PREC, XS, R, L, CC)                                                 \
+  if (precision == (PREC) && logm == (L) && C == (CC))                                 \
+    return kind == 0 ? launch_class<R, L, CC, XS>(kp, n, s) : launch_class_ss<R, L, CC, XS>(kp, n, s);
 #define GNLSE_C32(R, L, CC) GNLSE_CALL(GNLSE_FP32, false, R, L, CC)
 #define GNLSE_C64(R, L, CC) GNLSE_CALL(GNLSE_FP64, false, R, L, CC)
 #define GNLSE_CMX(R, L, CC) GNLSE_CALL(GNLSE_MIXED, true, R, L, CC)
@@ -115,6 +117,14 @@ cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, c
 #undef GNLSE_CMX
 #undef GNLSE_CALL
   return cudaErrorInvalidValue;
+}
+
+// the class's kernels its instances need, in one stream
+cudaError_t dispatch(int precision, int logm, int C, const KParams& kp, int n, cudaStream_t s, int kinds) {
+  cudaError_t e = cudaSuccess;
+  if ((kinds & 1) && (e = dispatch1(precision, logm, C, kp, n, s, 0)) != cudaSuccess) return e;
+  if ((kinds & 2) && (e = dispatch1(precision, logm, C, kp, n, s, 1)) != cudaSuccess) return e;
+  return e;
 }
 
 int ilog2i(int n) {
@@ -618,7 +628,9 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
     int j = k;
     while (j < n_instances && cls(ids[j]) == cls(ids[k]) && level(ids[j]) == level(ids[k])) ++j;
     const GridHost& g = p->grids[p->inst[ids[k]].grid];
-    p->classes.push_back({g.logm, g.C, k, j - k, level(ids[k])});
+    int kinds = 0;
+    for (int q = k; q < j; ++q) kinds |= p->inst[ids[q]].method <= GNLSE_SS_SYM_RK4 ? 1 : 2;
+    p->classes.push_back({g.logm, g.C, k, j - k, level(ids[k]), kinds});
     k = j;
   }
   cudaError_t e;
@@ -726,7 +738,7 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
     if (p->timing && (e = record_timing(p->t0[0], s)) != cudaSuccess) return cuda_fail(e);
-    e = dispatch(p->precision, c.logm, c.C, kp, c.count, s);
+    e = dispatch(p->precision, c.logm, c.C, kp, c.count, s, c.kinds);
     if (e != cudaSuccess) return cuda_fail(e);
     if (p->timing && (e = record_timing(p->t1[0], s)) != cudaSuccess) return cuda_fail(e);
     return GNLSE_OK;
@@ -739,7 +751,8 @@ int gnlse_propagate(gnlse_plan* p, void* d_fields, void* d_traces, double* d_tra
     kp.order = p->d_order + c.first;
     kp.n_order = c.count;
     if (p->timing && (e = record_timing(p->t0[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
-    if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k])) != cudaSuccess) return cuda_fail(e);
+    if ((e = dispatch(p->precision, c.logm, c.C, kp, c.count, p->side[k], c.kinds)) != cudaSuccess)
+      return cuda_fail(e);
     if (p->timing && (e = record_timing(p->t1[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaEventRecord(p->ev[k], p->side[k])) != cudaSuccess) return cuda_fail(e);
     if ((e = cudaStreamWaitEvent(s, p->ev[k], 0)) != cudaSuccess) return cuda_fail(e);

@@ -901,7 +901,7 @@ struct Engine {
   // Yb model inversion sums sum_k w_ratio |X_k|^2, sum_k w_sat |X_k|^2 of a spectrum
   // X = n fft(x) held in src (0: op.MA0, 1: op.acc, 2: the X buffer), over the cluster,
   // into out[0..1] (shared memory; written by thread 0 before the closing barrier)
-  static __device__ __noinline__ void yb_sums(const Ctx& cx, const GridDev& g, const Op& op, int src,
+  static __device__ __forceinline__ void yb_sums(const Ctx& cx, const GridDev& g, const Op& op, int src,
                                               double* out) {
     const double2* w = (const double2*)g.ybw;
     const int base = cx.rank * M;
@@ -1322,6 +1322,12 @@ struct Engine {
   //   adaptive: N(A) of S, 3 stages of rk4ip(S, h/2) -> Sh, N(A) of Sh,
   //             3 stages of rk4ip(Sh, h/2) -> Sf, 3 stages of rk4ip(S, h) -> Sh'
   //   fixed   : N(A) of S, 3 stages of rk4ip(S, h) -> S'
+  // Methods of the RK4IP stage loop (kernel kind 0): RK4IP fixed step, ARK4IP and
+  // ss_sym_rk4; the exponential split steps (kind 1) run in a kernel of their own, so that
+  // neither step loop's code weighs on the other's register allocation.
+  static __device__ __forceinline__ bool rk_method(int method) { return method <= 2; }
+
+  template <int KIND>
   static __device__ void run(const KParams& kp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cid = blockIdx.x / C;
@@ -1352,6 +1358,9 @@ struct Engine {
       c.yA[1][0] = c.yA[1][1] = c.yN[1][0] = c.yN[1][1] = 0.0;
     }
     __syncthreads();
+    // an instance of the other kernel's kind: every CTA of the cluster leaves here, before
+    // any cluster barrier
+    if (rk_method(c.d.method) != (KIND == 0)) return;
     const GridDev& g = c.g;
     const InstDev& d = c.d;
     InstState& st = c.st;
@@ -1414,9 +1423,8 @@ struct Engine {
       if (ssrk || sssimple) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
     }
 
-    // Solver.ss_symmetric: a step loop of its own, so that the main loop below keeps
-    // no call of its step function (its register allocation would suffer)
-    while (sssym && st.phase == 1 && budget > 0) {
+    // Solver.ss_symmetric / ss_simple / ss_reduced: the split-step kernel's loop
+    while (KIND == 1 && sssym && st.phase == 1 && budget > 0) {
       const double h = d.length / d.total_steps;
       const int sidx = st.sidx;
       ss_symmetric_step(cx, g, base + (long long)sidx * N, base + (long long)(sidx ^ 1) * N,
@@ -1427,7 +1435,7 @@ struct Engine {
       fixed_step_done(cx, kp, c, base, h);
     }
 
-    while (st.phase == 1 && budget > 0) {
+    while (KIND == 0 && st.phase == 1 && budget > 0) {
       // ---- one attempt (adaptive) or one step (fixed) ------------------------
       if (threadIdx.x == 0) {
         if (adaptive) {
@@ -1635,19 +1643,25 @@ struct Engine {
 template <class R, int LOGM, int C, bool XS>
 __global__ void __launch_bounds__(Engine<R, LOGM, C, XS>::T, Engine<R, LOGM, C, XS>::MINB)
     gnlse_kernel(KParams kp) {
-  Engine<R, LOGM, C, XS>::run(kp);
+  Engine<R, LOGM, C, XS>::template run<0>(kp);
 }
 
-// Host launcher for one (precision, M, C) class: one cluster per instance.
+// the exponential split-step methods (ss_symmetric, ss_simple, ss_reduced)
 template <class R, int LOGM, int C, bool XS>
-cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream) {
+__global__ void __launch_bounds__(Engine<R, LOGM, C, XS>::T, Engine<R, LOGM, C, XS>::MINB)
+    gnlse_ss_kernel(KParams kp) {
+  Engine<R, LOGM, C, XS>::template run<1>(kp);
+}
+
+// One cluster per instance of kernel k of class (R, M, C).
+template <class R, int LOGM, int C, bool XS>
+cudaError_t launch_kernel(void (*k)(KParams), const KParams& kp, int n_clusters, cudaStream_t stream) {
   using E = Engine<R, LOGM, C, XS>;
   const size_t smem = E::smem_bytes();
-  cudaError_t err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C, XS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   if (C > 8) {  // 16-CTA clusters are beyond the portable limit of 8
-    err = cudaFuncSetAttribute(gnlse_kernel<R, LOGM, C, XS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    err = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (err != cudaSuccess) return err;
   }
   cudaLaunchConfig_t cfg = {};
@@ -1666,7 +1680,18 @@ cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream)
   }
   cfg.attrs = attr;
   cfg.numAttrs = na;
-  return cudaLaunchKernelEx(&cfg, gnlse_kernel<R, LOGM, C, XS>, kp);
+  return cudaLaunchKernelEx(&cfg, k, kp);
+}
+
+// Host launchers for one (precision, M, C) class: the RK4IP-loop kernel, and the
+// split-step kernel.
+template <class R, int LOGM, int C, bool XS>
+cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream) {
+  return launch_kernel<R, LOGM, C, XS>(gnlse_kernel<R, LOGM, C, XS>, kp, n_clusters, stream);
+}
+template <class R, int LOGM, int C, bool XS>
+cudaError_t launch_class_ss(const KParams& kp, int n_clusters, cudaStream_t stream) {
+  return launch_kernel<R, LOGM, C, XS>(gnlse_ss_kernel<R, LOGM, C, XS>, kp, n_clusters, stream);
 }
 
 }  // namespace gnlse

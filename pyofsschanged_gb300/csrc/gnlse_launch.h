@@ -8,8 +8,12 @@
 
 namespace gnlse {
 
+// kernel of the RK4IP stage loop (RK4IP, ARK4IP, ss_sym_rk4)
 template <class R, int LOGM, int C, bool XS>
 cudaError_t launch_class(const KParams& kp, int n_clusters, cudaStream_t stream);
+// kernel of the exponential split steps (ss_symmetric, ss_simple, ss_reduced)
+template <class R, int LOGM, int C, bool XS>
+cudaError_t launch_class_ss(const KParams& kp, int n_clusters, cudaStream_t stream);
 
 // (precision, log2 M, C) classes compiled into the library.
 #ifdef GNLSE_ENSEMBLE_SUBSET
