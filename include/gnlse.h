@@ -63,18 +63,26 @@ enum {
 };
 
 /* Methods: Solver.rk4ip with the fixed-step or the adaptive (step-doubling) driver;
- * with the fixed-step driver, Solver.ss_sym_rk4 (pyofss/modules/solver.py:330-337: linear
- * half step, classical RK4 on the nonlinear term, linear half step) and
- * Solver.ss_symmetric (solver.py:267-275: linear half step, exponential nonlinear step
- * evaluated with the unpropagated field, linear half step; not with self-steepening,
- * whose exponent in the reference divides by the field).  Neither split step runs with
- * gain or the Yb model (GNLSE_UNSUPPORTED). */
+ * the split steps Solver.ss_sym_rk4 (pyofss/modules/solver.py:330-337: linear half step,
+ * classical RK4 on the nonlinear term, linear half step), Solver.ss_symmetric
+ * (solver.py:267-275: linear half step, exponential nonlinear step evaluated with the
+ * unpropagated field, linear half step; not with self-steepening, whose exponent in the
+ * reference divides by the field), ss_simple, ss_reduced, ss_sym_midpoint and
+ * ss_agrawal, with the fixed-step driver or -- a split-step method OR'ed with
+ * GNLSE_ADAPTIVE, the reference's "a"-prefixed methods (stepper.py:111-116) -- the
+ * adaptive driver with the method's order from Solver.errors (solver.py:57-70).  No
+ * split step runs with gain or the Yb model (GNLSE_UNSUPPORTED). */
 enum {
   GNLSE_RK4IP = 0, GNLSE_ARK4IP = 1, GNLSE_SS_SYM_RK4 = 2, GNLSE_SS_SYMMETRIC = 3,
   GNLSE_SS_SIMPLE = 4,  /* Solver.ss_simple (solver.py:256-265): exponential nonlinear step, then a
                            full linear step; fixed step, no gain, no self-steepening */
-  GNLSE_SS_REDUCED = 5  /* Solver.ss_reduced (solver.py:277-287): ss_symmetric with the exponent
-                           from the half-step-propagated field; same limits */
+  GNLSE_SS_REDUCED = 5,  /* Solver.ss_reduced (solver.py:277-287): ss_symmetric with the exponent
+                            from the half-step-propagated field; same limits */
+  GNLSE_SS_SYM_MIDPOINT = 6,  /* Solver.ss_sym_midpoint (solver.py:323-328): linear half step,
+                                 Solver.midpoint on the nonlinear term, linear half step */
+  GNLSE_SS_AGRAWAL = 7,       /* Solver.ss_agrawal (solver.py:290-320): iterated symmetric split
+                                 step with the exponent n(Y)/Y (0 where |Y| <= 1e-5) */
+  GNLSE_ADAPTIVE = 16         /* flag: the adaptive step-doubling driver for a split step */
 };
 /* precision: GNLSE_FP32 complex64 throughout (fields complex64);
  * GNLSE_FP64 complex128 throughout (fields complex128);

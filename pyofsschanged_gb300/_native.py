@@ -27,6 +27,9 @@ GNLSE_SS_SYM_RK4 = 2
 GNLSE_SS_SYMMETRIC = 3
 GNLSE_SS_SIMPLE = 4
 GNLSE_SS_REDUCED = 5
+GNLSE_SS_SYM_MIDPOINT = 6
+GNLSE_SS_AGRAWAL = 7
+GNLSE_ADAPTIVE = 16
 GNLSE_FP32 = 0
 GNLSE_FP64 = 1
 GNLSE_MIXED = 2

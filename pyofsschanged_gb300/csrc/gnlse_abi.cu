@@ -477,19 +477,22 @@ int gnlse_plan_create(int precision, int n_grids, const gnlse_grid_desc* grids, 
   int64_t foff = 0, soff = 0, toff = 0, zoff = 0;
   for (int i = 0; i < n_instances; ++i) {
     const gnlse_instance_desc& id = instances[i];
-    if (id.grid < 0 || id.grid >= n_grids ||
-        id.method < GNLSE_RK4IP || id.method > GNLSE_SS_REDUCED ||
+    // base method and the adaptive flag (split steps only; GNLSE_ARK4IP is adaptive RK4IP)
+    const int bm = id.method & ~GNLSE_ADAPTIVE;
+    const bool flagged = (id.method & GNLSE_ADAPTIVE) != 0;
+    if (id.grid < 0 || id.grid >= n_grids || bm < GNLSE_RK4IP || bm > GNLSE_SS_AGRAWAL ||
+        (flagged && bm < GNLSE_SS_SYM_RK4) ||
         id.total_steps < 1 || id.traces < 1 || id.max_traces < 0 || !(id.length >= 0) ||
-        (id.method == GNLSE_ARK4IP && !(id.local_error > 0))) {
+        ((id.method == GNLSE_ARK4IP || flagged) && !(id.local_error > 0))) {
       free_plan(p);
       return GNLSE_BAD_ARGUMENT;
     }
-    const bool split = id.method >= GNLSE_SS_SYM_RK4;
+    const bool split = bm >= GNLSE_SS_SYM_RK4;
     if (split && (grids[id.grid].gain_on || grids[id.grid].yb_on)) {
       free_plan(p);  // the split-step paths have no amplifier step
       return GNLSE_UNSUPPORTED;
     }
-    if (id.method >= GNLSE_SS_SYMMETRIC && grids[id.grid].ss_w) {
+    if (bm >= GNLSE_SS_SYMMETRIC && bm <= GNLSE_SS_REDUCED && grids[id.grid].ss_w) {
       free_plan(p);  // exponential step with self-steepening (see gnlse.h)
       return GNLSE_UNSUPPORTED;
     }

@@ -672,7 +672,9 @@ struct Engine {
   // |x|^2, on exit X holds G+(x R(x)) (spectral).  The transforms carry only
   // light per-element work in their first / last passes; with want_e the
   // Simpson energy (nJ) of x is returned.
-  static __device__ __forceinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e) {
+  // keep_x (split-step kernel): also store x, sample n at keep_x[n]
+  static __device__ __forceinline__ double nonlinear(const Ctx& cx, const GridDev& g, bool want_e,
+                                                     V* keep_x = nullptr) {
     const R invN = (R)(1.0 / (double)N);
     const bool raman = g.raman != 0;
     V* X = cx.X;
@@ -687,6 +689,7 @@ struct Engine {
       V x = cscale(v, invN);
       R p = cabs2(x);
       if (keep_p) P[s] = mk<V>(p, (R)0);
+      if (keep_x) keep_x[n1 * M + n2] = x;
       X[s] = raman ? x : cscale(x, p);
     };
     // The P buffers are free here (their last use, the Raman inverse or an energy
@@ -1072,7 +1075,7 @@ struct Engine {
     const int base = cx.rank * M;
     V* X = cx.X;
     V* P = cx.P;
-    {  // S_L = E S -> Sh
+    if (E) {  // S_L = E S -> Sh
       struct In { SL e, s; };
       each_slot<4, In>([&](int l) { return In{lds(E, base + l), lds(S, base + l)}; },
                        [&](int l, const In& r) {
@@ -1082,6 +1085,9 @@ struct Engine {
                            Sh[base + l] = cmul(r.e, r.s);
                          }
                        });
+      __syncthreads();
+    } else {  // no first linear step (ss_simple): S_L = S
+      each_slot<4, SL>([&](int l) { return lds(S, base + l); }, [&](int l, const SL& v) { sts(Sh, base + l, v); });
       __syncthreads();
     }
     auto rdSh = [&](int o, int l) -> V { return ldv(Sh, o * M + l); };
@@ -1147,6 +1153,203 @@ struct Engine {
       }
     };
     fwd(cx, X, rdXt, wrS);
+  }
+
+  // ---- split-step kernel: the remaining step methods and their adaptive driver ----
+  static __device__ __forceinline__ SL sl_mul(const SL& a, const SL& b) {
+    if constexpr (XS) {
+      return dfc_mul(a, b);
+    } else {
+      return cmul(a, b);
+    }
+  }
+  static __device__ __forceinline__ SL sl_add(const SL& a, const V& b) {
+    if constexpr (XS) {
+      return dfc_add_f(a, b);
+    } else {
+      return cadd(a, b);
+    }
+  }
+  static __device__ __forceinline__ void sts(SV* p, int a, const SL& v) {
+    if constexpr (XS) {
+      dfc_store(p, a, v);
+    } else {
+      p[a] = v;
+    }
+  }
+  // nonlinear operator shared by every step of the split-step kernel (one copy of its code)
+  static __device__ __noinline__ void nonlinear_ss(const Ctx& cx, const GridDev& g, V* keep_x) {
+    nonlinear(cx, g, false, keep_x);
+  }
+
+  // Solver.ss_sym_midpoint / ss_sym_rk4 (solver.py:323-337) with Solver.midpoint / rk4
+  // (solver.py:101-116) on the nonlinear term, on the spectral state:
+  //   S_L = E S;  k_j = h N(S_L + c_j k_{j-1});  S' = E (S_L + sum_j b_j k_j)
+  // NS = 2: midpoint (c = 0, 1/2; b = 0, 1); NS = 4: classical RK4.  acc: RK4 sum.
+  template <int NS>
+  static __device__ __forceinline__ void ss_rk_step(const Ctx& cx, const GridDev& g, const SV* S, SV* Sh,
+                                                    SV* acc, const SV* E, double hd) {
+    const int base = cx.rank * M;
+    V* X = cx.X;
+    const R* Kr = (const R*)g.Kr;
+    const R h = (R)hd, half = (R)0.5, sixth = (R)(1.0 / 6.0), third = (R)(1.0 / 3.0);
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      const SL sl = sl_mul(lds(E, a), lds(S, a));
+      sts(Sh, a, sl);
+      X[pad(l)] = slhi(sl);
+    }
+    __syncthreads();
+    for (int j = 0; j < NS; ++j) {
+      nonlinear_ss(cx, g, nullptr);
+      for (int l = threadIdx.x; l < M; l += T) {
+        const int a = base + l;
+        const V k = ik(h * ldro(&Kr[a]), X[pad(l)]);
+        const SL sl = lds(Sh, a);
+        if (NS == 2) {
+          if (j == 0) {
+            X[pad(l)] = cadd(slhi(sl), cscale(k, half));
+          } else {
+            sts(Sh, a, sl_mul(lds(E, a), sl_add(sl, k)));
+          }
+        } else if (j == 0) {
+          sts(acc, a, sl_add(sl, cscale(k, sixth)));
+          X[pad(l)] = cadd(slhi(sl), cscale(k, half));
+        } else if (j < 3) {
+          sts(acc, a, sl_add(lds(acc, a), cscale(k, third)));
+          X[pad(l)] = cadd(slhi(sl), j == 1 ? cscale(k, half) : k);
+        } else {
+          sts(Sh, a, sl_mul(lds(E, a), sl_add(lds(acc, a), cscale(k, sixth))));
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ss_agrawal's ratio n(y)/y where |y| > 1e-5, else 0 (solver.py:295-316), in FP64
+  // (out of line: FP64 library code, called from every transform epilogue site)
+  static __device__ __noinline__ V agr_ratio(V n, V y) {
+    const double yr = (double)y.x, yi = (double)y.y;
+    if (!(hypot(yr, yi) > 1.0e-5)) return mk<V>(R(0.0), R(0.0));
+    const double nr = (double)n.x, ni = (double)n.y, d = yr * yr + yi * yi;
+    return mk<V>(R((nr * yr + ni * yi) / d), R((ni * yr - nr * yi) / d));
+  }
+  // exp(hh r) - 1 = expm1(x) cos y - 2 sin^2(y/2) + i e^x sin y, x + i y = hh r, in FP64
+  static __device__ __noinline__ V cexpm1_scaled(double hh, V r) {
+    const double x = hh * (double)r.x, y = hh * (double)r.y;
+    double sn, cs;
+    sincos(y, &sn, &cs);
+    const double hs = sin(0.5 * y), em1 = expm1(x);
+    return mk<V>(R(em1 * cs - 2.0 * hs * hs), R((em1 + 1.0) * sn));
+  }
+
+  // Solver.ss_agrawal (solver.py:290-320), with r(Y) = n(Y)/Y (0 where |Y| <= 1e-5):
+  //   A_L = L(A, h/2);  Y_1 = L(exp(h r(A)) A_L, h/2);  S' = L(exp(h/2 (r(Y_1) + r(A))) A_L, h/2)
+  // in the spectral state, each exponential step as S_L + G+((exp(.) - 1) a_L) so that a
+  // small nonlinear phase keeps the state's precision.  Time-domain scratch (N samples
+  // each): y (the field whose ratio is taken, then Delta_2), rA = r(A), aL = a_L.
+  static __device__ __forceinline__ void ss_agrawal_step(const Ctx& cx, const GridDev& g, const SV* S, SV* Sh,
+                                                         V* y, V* rA, V* aL, const SV* E, double h) {
+    const int base = cx.rank * M;
+    const R invN = (R)(1.0 / (double)N);
+    V* X = cx.X;
+    const R* Kr = (const R*)g.Kr;
+    auto rdKX = [&](int, int l) -> V { return ik(ldro(&Kr[base + l]), X[pad(l)]); };
+    // r(A): x -> y and X = G+(x R(x)) by the nonlinear operator, n(A) = G-(i K X)/N
+    load_state(cx, S);
+    nonlinear_ss(cx, g, y);
+    auto wr_rA = [&](int n1, int n2, V v) {
+      const int t = n1 * M + n2;
+      rA[t] = agr_ratio(cscale(v, invN), y[t]);
+    };
+    inv(cx, X, rdKX, wr_rA);
+    // S_L = E S -> Sh, a_L = G-(S_L)/N
+    auto rdSL = [&](int, int l) -> V {
+      const int a = base + l;
+      const SL sl = sl_mul(lds(E, a), lds(S, a));
+      sts(Sh, a, sl);
+      return slhi(sl);
+    };
+    auto wr_aL = [&](int n1, int n2, V v) { aL[n1 * M + n2] = cscale(v, invN); };
+    inv(cx, X, rdSL, wr_aL);
+    // Y_1 = E (S_L + G+((exp(h r(A)) - 1) a_L)) into X, the nonlinear operator's input
+    auto rdD1 = [&](int n1, int n2) -> V {
+      const int t = n1 * M + n2;
+      return cmul(cexpm1_scaled(h, rA[t]), aL[t]);
+    };
+    auto wrY1 = [&](int, int l, V v) {
+      const int a = base + l;
+      X[pad(l)] = slhi(sl_mul(lds(E, a), sl_add(lds(Sh, a), v)));
+    };
+    fwd(cx, X, rdD1, wrY1);
+    // r(Y_1), then Delta_2 = (exp(h/2 (r(Y_1) + r(A))) - 1) a_L into y
+    nonlinear_ss(cx, g, y);
+    auto wrD2 = [&](int n1, int n2, V v) {
+      const int t = n1 * M + n2;
+      const V r1 = agr_ratio(cscale(v, invN), y[t]);
+      y[t] = cmul(cexpm1_scaled(0.5 * h, cadd(r1, rA[t])), aL[t]);
+    };
+    inv(cx, X, rdKX, wrD2);
+    // S' = E (S_L + G+(Delta_2))
+    auto rdD2 = [&](int n1, int n2) -> V { return y[n1 * M + n2]; };
+    auto wrS = [&](int, int l, V v) {
+      const int a = base + l;
+      sts(Sh, a, sl_mul(lds(E, a), sl_add(lds(Sh, a), v)));
+    };
+    fwd(cx, X, rdD2, wrS);
+  }
+
+  // one step of split-step method sm from S to Sh; E = exp(hD/2) (exp(hD) for
+  // ss_simple); tmp: three N-element scratch slots.  Out of line: the fixed and the
+  // adaptive driver call it from four sites.
+  static __device__ __noinline__ void ss_step(const Ctx& cx, const GridDev& g, int sm, const SV* S, SV* Sh,
+                                              SV* tmp, const SV* E, double h) {
+    if (sm >= 3 && sm <= 5) {
+      ss_symmetric_step(cx, g, S, Sh, reinterpret_cast<V*>(tmp), sm == 4 ? nullptr : E, E, h, sm == 5);
+    } else if (sm == 2) {
+      ss_rk_step<4>(cx, g, S, Sh, tmp, E, h);
+    } else if (sm == 6) {
+      ss_rk_step<2>(cx, g, S, Sh, tmp, E, h);
+    } else {
+      ss_agrawal_step(cx, g, S, Sh, reinterpret_cast<V*>(tmp), reinterpret_cast<V*>(tmp + N),
+                      reinterpret_cast<V*>(tmp + 2 * N), E, h);
+    }
+  }
+
+  // Solver.errors (solver.py:57-70): the order of each split step in the adaptive driver
+  static __device__ __forceinline__ int ss_order(int sm) {
+    return (sm == 4 || sm == 5) ? 2 : (sm == 2 ? 5 : 3);
+  }
+
+  // step-doubling error norms of F (fine) against Cc (coarse) over the cluster, and the
+  // local extrapolation fa F - fb Cc into Cc (stepper.py:231-245, 272-274, 338)
+  static __device__ void ss_extrapolate(const Ctx& cx, const SV* F, SV* Cc, double fa, double fb, double (&s)[3]) {
+    const int base = cx.rank * M;
+    double d2 = 0.0, f2 = 0.0, bad = 0.0;
+    for (int l = threadIdx.x; l < M; l += T) {
+      const int a = base + l;
+      if constexpr (XS) {
+        const dfc f = dfc_load(F, a), c = dfc_load(Cc, a);
+        const double fr = df_to_double(f.re), fi = df_to_double(f.im);
+        const double dr = fr - df_to_double(c.re), di = fi - df_to_double(c.im);
+        d2 += dr * dr + di * di;
+        f2 += fr * fr + fi * fi;
+        if (!isfinite(f.re.hi) || !isfinite(f.im.hi)) bad = 1.0;
+        dfc_store(Cc, a, dfc_add(dfc_scale(f, df_from_double(fa)), dfc_scale(c, df_from_double(-fb))));
+      } else {
+        const V f = F[a], c = Cc[a];
+        const double fr = (double)f.x, fi = (double)f.y;
+        const double dr = fr - (double)c.x, di = fi - (double)c.y;
+        d2 += dr * dr + di * di;
+        f2 += fr * fr + fi * fi;
+        if (!isfinite(fr) || !isfinite(fi)) bad = 1.0;
+        Cc[a] = mk<V>(R(fa) * f.x - R(fb) * c.x, R(fa) * f.y - R(fb) * c.y);
+      }
+    }
+    s[0] = d2;
+    s[1] = f2;
+    s[2] = bad;
+    cluster_sum<3>(cx, s);
   }
 
   // dst = E dst over this CTA's slice: the linear half steps of the split-step method
@@ -1378,7 +1581,7 @@ struct Engine {
 
     if (st.phase == 0) {
       int ntr = 0, ovf = 0;
-      if (d.method == 1 && d.traces != 1) {
+      if ((d.method == 1 || (d.method & 16)) && d.traces != 1) {
         if (d.max_traces > 0) {
           FV* tr = (FV*)kp.traces + d.trace_off;
           for (int l = threadIdx.x; l < M; l += T) tr[cx.rank * M + l] = field[cx.rank * M + l];
@@ -1398,7 +1601,7 @@ struct Engine {
         st.Nph_in = n_in;
         st.sidx = 0;
         st.z = 0.0;
-        st.h = d.method == 1 ? d.h0 : d.length / d.total_steps;
+        st.h = (d.method == 1 || (d.method & 16)) ? d.h0 : d.length / d.total_steps;
         st.z_ignore = d.length / d.traces;
         st.ma_valid = 0;
         st.ta = 0;
@@ -1410,29 +1613,109 @@ struct Engine {
     }
 
     const bool adaptive = d.method == 1;
-    // Solver.ss_sym_rk4 (solver.py:330-337): S <- E S, classical RK4 on the nonlinear
-    // term (the RK4IP stage algebra with the exp(hD/2) factors replaced by an exact 1,
-    // table 6), result <- E result, E = exp(hD/2) (table 7)
+    // Solver.ss_sym_rk4 (solver.py:330-337), fixed step: S <- E S, classical RK4 on the
+    // nonlinear term (the RK4IP stage algebra with the exp(hD/2) factors replaced by an
+    // exact 1, table 6), result <- E result, E = exp(hD/2) (table 7)
     const bool ssrk = d.method == 2;
-    // Solver.ss_symmetric (3), ss_simple (4), ss_reduced (5): ss_symmetric_step
-    const bool sssym = d.method >= 3;
-    const bool sssimple = d.method == 4;
-    if (st.phase == 1 && !adaptive) {
-      // exp(hD/2), or exp(hD) for ss_simple, whose one linear step spans the step
-      exp_table(cx, g, (sssimple ? 1.0 : 0.5) * (d.length / d.total_steps), base + 7 * N, nullptr);
-      if (ssrk || sssimple) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
+    if (KIND == 0 && st.phase == 1 && !adaptive) {
+      exp_table(cx, g, 0.5 * (d.length / d.total_steps), base + 7 * N, nullptr);
+      if (ssrk) exp_table(cx, g, 0.0, base + 6 * N, nullptr);
     }
 
-    // Solver.ss_symmetric / ss_simple / ss_reduced: the split-step kernel's loop
-    while (KIND == 1 && sssym && st.phase == 1 && budget > 0) {
-      const double h = d.length / d.total_steps;
-      const int sidx = st.sidx;
-      ss_symmetric_step(cx, g, base + (long long)sidx * N, base + (long long)(sidx ^ 1) * N,
-                        reinterpret_cast<V*>(base + 2 * N), base + (sssimple ? 6 : 7) * N, base + 7 * N, h,
-                        d.method == 5);
-      if (threadIdx.x == 0) st.evals += 1;
-      budget -= 1;
-      fixed_step_done(cx, kp, c, base, h);
+    if constexpr (KIND == 1) {
+      // Split steps (method & 15): ss_symmetric (3), ss_simple (4), ss_reduced (5),
+      // ss_sym_midpoint (6), ss_agrawal (7), and with the adaptive flag (16) also
+      // ss_sym_rk4 (2).  Scratch: state slots 0/1, fine step 2, step scratch 3-5,
+      // exp(hD) tables 6-7.
+      const int sm = d.method & 15;
+      const bool sadapt = (d.method & 16) != 0;
+      SV* tmp = base + 3 * N;
+      if (!sadapt) {
+        // fixed step (stepper.py:164-221): exp(hD/2), or exp(hD) for ss_simple
+        const double hf = d.length / d.total_steps;
+        if (st.phase == 1) exp_table(cx, g, (sm == 4 ? 1.0 : 0.5) * hf, base + 7 * N, nullptr);
+        while (st.phase == 1 && budget > 0) {
+          const int sidx = st.sidx;
+          ss_step(cx, g, sm, base + (long long)sidx * N, base + (long long)(sidx ^ 1) * N, tmp, base + 7 * N, hf);
+          if (threadIdx.x == 0) st.evals += 1;
+          budget -= 1;
+          fixed_step_done(cx, kp, c, base, hf);
+        }
+      }
+      // adaptive step doubling (stepper.py:247-376) with the method's order (Solver.errors)
+      while (sadapt && st.phase == 1 && budget > 0) {
+        if (threadIdx.x == 0 && st.ta == 0) {
+          if (st.steps >= 99999) {
+            st.status = ST_MAX_STEPS;
+            st.phase = 2;
+          } else if (st.z + st.h > d.length) {
+            st.h = d.length - st.z;
+          }
+        }
+        __syncthreads();
+        if (st.phase != 1) break;
+        const double h = st.h;
+        const int sidx = st.sidx;
+        SV* S = base + (long long)sidx * N;
+        SV* Cc = base + (long long)(sidx ^ 1) * N;
+        SV* F = base + 2 * N;
+        // half steps' linear factor (table 6) and the coarse step's (table 7)
+        exp_table(cx, g, (sm == 4 ? 0.5 : 0.25) * h, base + 6 * N, base + 7 * N);
+        ss_step(cx, g, sm, S, Cc, tmp, base + 6 * N, 0.5 * h);  // A_half
+        ss_step(cx, g, sm, Cc, F, tmp, base + 6 * N, 0.5 * h);  // A_fine
+        ss_step(cx, g, sm, S, Cc, tmp, base + 7 * N, h);        // A_coarse
+        const int eta = ss_order(sm);
+        const double f_eta = (double)(1 << (eta - 1));
+        double nrm[3];
+        ss_extrapolate(cx, F, Cc, f_eta / (f_eta - 1.0), 1.0 / (f_eta - 1.0), nrm);
+        budget -= 1;
+        double delta;  // relative_local_error (stepper.py:231-245)
+        if (nrm[2] != 0.0 || !isfinite(nrm[1])) {
+          delta = 1.0;
+        } else {
+          const double nf = sqrt(nrm[1]);
+          delta = nf != 0.0 ? sqrt(nrm[0]) / nf : sqrt(nrm[0]);
+        }
+        const bool accept = delta < 2.0 * d.tol;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          st.evals += 3;
+          st.attempts += 1;
+          st.ta += 1;
+          st.delta_last = delta;
+          if (delta > 0.0) {
+            st.h = h * fmin(10.0, fmax(0.2, 0.9 * pow(d.tol / delta, 1.0 / (double)eta)));
+          } else {
+            st.h = h * 10.0;
+          }
+          if (accept) {
+            st.z += h;
+            st.sidx ^= 1;  // Cc holds the extrapolated solution
+            st.accepted += 1;
+            st.steps += 1;
+            st.ta = 0;
+            if (st.z >= d.length) {
+              st.status = ST_OK;
+              st.phase = 2;
+            }
+          } else {
+            st.rejected += 1;
+            if (st.h < 1e-37) {
+              st.status = ST_SMALL_STEP;
+              st.phase = 2;
+            } else if (st.ta >= 1000) {
+              st.status = ST_SUITABLE_STEP;
+              st.phase = 2;
+            }
+          }
+        }
+        __syncthreads();
+        if (accept && st.z > st.z_ignore) {
+          store_trace(cx, kp, c, base + (long long)st.sidx * N, st.z);
+          if (threadIdx.x == 0) st.z_ignore += d.length / d.traces;
+          __syncthreads();
+        }
+      }
     }
 
     while (KIND == 0 && st.phase == 1 && budget > 0) {

@@ -19,7 +19,10 @@ PRECISIONS = {"fp32": nat.GNLSE_FP32, "fp64": nat.GNLSE_FP64, "mixed": nat.GNLSE
               "df": nat.GNLSE_DF}
 METHODS = {"rk4ip": nat.GNLSE_RK4IP, "ark4ip": nat.GNLSE_ARK4IP, "ss_sym_rk4": nat.GNLSE_SS_SYM_RK4,
            "ss_symmetric": nat.GNLSE_SS_SYMMETRIC, "ss_simple": nat.GNLSE_SS_SIMPLE,
-           "ss_reduced": nat.GNLSE_SS_REDUCED}
+           "ss_reduced": nat.GNLSE_SS_REDUCED, "ss_sym_midpoint": nat.GNLSE_SS_SYM_MIDPOINT,
+           "ss_agrawal": nat.GNLSE_SS_AGRAWAL}
+# the reference's adaptive split steps ("a" + method, stepper.py:111-116)
+METHODS.update({"a" + k: v | nat.GNLSE_ADAPTIVE for k, v in list(METHODS.items()) if k.startswith("ss_")})
 
 
 def _ptr(a):
@@ -45,7 +48,7 @@ class Instance:
         if max_traces is None:
             if self.traces == 1:
                 max_traces = 0
-            elif self.method != "ark4ip":  # fixed-step trace rule
+            elif not self.method.startswith("a"):  # fixed-step trace rule
                 step = self.total_steps // self.traces if self.traces else 0
                 max_traces = (self.total_steps + step - 1) // step if step > 0 else 0
             else:

@@ -6,10 +6,13 @@ propagates the field through the fibre and returns it, as
 ``Fibre.__call__`` does (fibre.py:136-148).  ``method`` selects the engine
 path: ``"cuda_rk4ip"`` / ``"rk4ip"`` (fixed step, ``total_steps`` steps),
 ``"cuda_ark4ip"`` / ``"ark4ip"`` (adaptive step doubling with tolerance
-``local_error``), or the fixed-step split-step methods ``"ss_sym_rk4"``,
-``"ss_symmetric"``, ``"ss_simple"`` and ``"ss_reduced"`` (pyofss/modules/solver.py:256-287,330-337).  ``precision`` selects ``"mixed"`` (default: complex64
-transforms with a double-float propagation state), ``"fp32"`` (complex64
-throughout) or ``"fp64"`` (complex128 throughout).  The stepper exceptions of
+``local_error``), or the split-step methods ``"ss_sym_rk4"``, ``"ss_symmetric"``,
+``"ss_simple"``, ``"ss_reduced"``, ``"ss_sym_midpoint"`` and ``"ss_agrawal"``
+(pyofss/modules/solver.py:256-337) with the fixed-step driver, or, "a"-prefixed
+(``"ass_symmetric"`` ...), with the adaptive one.  ``precision`` selects ``"mixed"``
+(default: complex64 transforms with a double-float propagation state), ``"df"``
+(double-float throughout), ``"fp32"`` (complex64 throughout) or ``"fp64"``
+(complex128 throughout).  The stepper exceptions of
 pyofss/modules/stepper.py:33-47 are raised with the same names.
 
 The saturable amplifier and the Yb two-level gain (``use_Yb_model``; its cross
@@ -27,7 +30,7 @@ import torch
 
 from . import _native as nat
 from .characteristics import trace_characteristics
-from .engine import Instance, Plan
+from .engine import METHODS, Instance, Plan
 from .operators import GridTables
 
 
@@ -124,7 +127,7 @@ class Storage:
 class _StepperView:
     def __init__(self, method, traces, local_error, total_steps, length):
         self.method = method
-        self.adaptive = method == "ark4ip"
+        self.adaptive = method.startswith("a")
         self.traces = traces
         self.local_error = local_error
         self.total_steps = total_steps
@@ -145,10 +148,9 @@ class Fibre:
         m = method.lower()
         if m.startswith("cuda_"):
             m = m[5:]
-        if m not in ("rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric", "ss_simple", "ss_reduced"):
+        if m not in METHODS:
             raise NotImplementedError(
-                f"method {method!r}: the CUDA engine runs rk4ip / ark4ip / ss_sym_rk4 / ss_symmetric / "
-                "ss_simple / ss_reduced")
+                f"method {method!r}: the CUDA engine runs {' / '.join(METHODS)}")
         if sim_type not in (None, "default"):
             raise NotImplementedError("sim_type='wdm' is not on the CUDA path")
         if raman_scattering and not use_all and self_steepening:
@@ -161,9 +163,9 @@ class Fibre:
                 raise Exception("Repetition rate is not defined.")
             E_sat = P_sat * Tr
         gain = use_Yb_model or (small_signal_gain is not None and E_sat is not None)
-        if gain and m.startswith("ss_"):
+        if gain and m.startswith(("ss_", "ass_")):
             raise NotImplementedError("the split-step methods run without gain on the CUDA path")
-        if self_steepening and m in ("ss_symmetric", "ss_simple", "ss_reduced"):
+        if self_steepening and m.lstrip("a") in ("ss_symmetric", "ss_simple", "ss_reduced"):
             # the reference's exponential step divides by the field (nonlinearity.py:230-234)
             raise NotImplementedError(f"{m} with self-steepening is not on the CUDA path")
         self.name = name

@@ -20,7 +20,9 @@ def names():
 
 
 # methods of the reference that the CUDA engine runs (the oracle restates more)
-ENGINE_METHODS = {"rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric", "ss_simple", "ss_reduced"}
+ENGINE_METHODS = {"rk4ip", "ark4ip", "ss_sym_rk4", "ss_symmetric", "ss_simple", "ss_reduced",
+                  "ss_sym_midpoint", "ss_agrawal", "ass_sym_rk4", "ass_symmetric", "ass_simple",
+                  "ass_reduced", "ass_sym_midpoint", "ass_agrawal"}
 
 
 def engine_names():

@@ -85,7 +85,7 @@ def test_fp32_matches_reference(cuda_ready, name):
     case = gc.load(name)
     plan, out, st = run(case, "fp32")
     assert st["status"] == 0 and st["finished"] == 1
-    split = case["params"]["fibre"]["method"].startswith("ss_")
+    split = case["params"]["fibre"]["method"].startswith(("ss_", "ass_"))
     tol = 1e-3 if name in CHAOTIC else (FP32_SPLIT_STEP_TOL if split else FP32_SPEC_TOL)
     assert spec_err(out, case["A_out"]) <= tol
     # the step-size controller sees FP32 round-off; the attempt count stays close
@@ -118,7 +118,7 @@ def test_cluster_paths_match_reference(cuda_ready, name, precision, cluster):
     elif precision == "mixed":
         assert spec_err(out, case["A_out"]) <= FP32_SPEC_TOL
     else:
-        split = case["params"]["fibre"]["method"].startswith("ss_")
+        split = case["params"]["fibre"]["method"].startswith(("ss_", "ass_"))
         assert spec_err(out, case["A_out"]) <= (FP32_SPLIT_STEP_TOL if split else FP32_SPEC_TOL)
 
 

@@ -188,7 +188,8 @@ def test_fibre_model_options_on_the_cuda_path():
     Fibre(length=1e-5, beta=[0, 0, -10.0], gamma=100.0, raman_scattering=True, method="cuda_ark4ip")
     Fibre(length=1e-3, beta=[0, 0, 25.0], gamma=5.0, use_Yb_model=True, Pp_0=1.0, N=1.0, Rr=1e-5,
           method="cuda_rk4ip")
-    for m in ("ss_simple", "ss_reduced", "ss_symmetric", "ss_sym_rk4"):
+    for m in ("ss_simple", "ss_reduced", "ss_symmetric", "ss_sym_rk4", "ss_sym_midpoint", "ss_agrawal",
+              "ass_symmetric", "ass_sym_rk4", "ass_agrawal"):
         Fibre(length=1e-5, beta=[0, 0, -10.0], gamma=100.0, method=m)
     with pytest.raises(NotImplementedError):
         Fibre(length=1e-5, gamma=100.0, raman_scattering=True, self_steepening=True)
@@ -197,7 +198,9 @@ def test_fibre_model_options_on_the_cuda_path():
     with pytest.raises(NotImplementedError):
         Fibre(length=1e-3, gamma=5.0, use_Er_profile=True)
     with pytest.raises(NotImplementedError):
-        Fibre(length=1e-3, gamma=5.0, method="ss_agrawal")
+        Fibre(length=1e-3, gamma=5.0, method="ss_euler")
+    with pytest.raises(NotImplementedError):
+        Fibre(length=1e-3, gamma=5.0, self_steepening=True, method="ass_symmetric")
     with pytest.raises(NotImplementedError):
         Fibre(length=1e-3, gamma=5.0, small_signal_gain=10.0, E_sat=1.0, method="ss_sym_rk4")
     with pytest.raises(NotImplementedError):
