@@ -207,6 +207,43 @@ def batched_library_leg(a, members, domains, fields, stats, value, dev):
                       "counts, grids one after another"}
 
 
+def replay_experiment(a, members, domains, fields, leg_out, local, count=8):
+    """The mixed mode's worst members re-run on the fp64 plan's own accepted step sequence
+    (gnlse_set_replay): their error against fp64 with the step-size decisions taken out,
+    beside the error of the mixed run with its own controller."""
+    import numpy as np
+    from pyofsschanged_gb300.engine import Plan
+    from pyofsschanged_gb300.ensemble import ensemble_plan_inputs
+    ref, mixed = leg_out["fp64"], leg_out["mixed"]
+
+    def err(o, r):
+        return float(np.linalg.norm(np.fft.ifft(o) - np.fft.ifft(r)) / np.linalg.norm(np.fft.ifft(r)))
+
+    worst = sorted(range(len(members)), key=lambda i: -err(mixed[i], ref[i]))[:count]
+    sub = [members[i] for i in worst]
+    g, inst = ensemble_plan_inputs(sub, {n: domains[n] for n in set(m.n for m in sub)})
+    p64 = Plan(g, inst, precision="fp64", device=local)
+    for j in range(len(sub)):
+        p64.set_step_log(j, 100000)
+    f64 = p64.pack([fields[i] for i in worst])
+    p64.propagate(f64)
+    st64 = p64.stats()
+    logs = [p64.step_log(j, st64) for j in range(len(sub))]
+    out64 = [x.cpu().numpy() for x in p64.unpack(f64)]
+    pm = Plan(g, inst, precision="mixed", device=local)
+    for j in range(len(sub)):
+        pm.set_replay(j, logs[j][:, 1])
+    fm = pm.pack([fields[i] for i in worst])
+    pm.propagate(fm)
+    outm = [x.cpu().numpy().astype(complex) for x in pm.unpack(fm)]
+    rows = {}
+    for j, i in enumerate(worst):
+        rows[str(i)] = {"n": members[i].n, "steps": int(len(logs[j])),
+                        "mixed_own_controller": float("%.3e" % err(mixed[i], ref[i])),
+                        "mixed_on_fp64_steps": float("%.3e" % err(outm[j], out64[j]))}
+    return rows
+
+
 def amplifier_leg(local):
     """The 2^16-point amplifier (pyofsschanged_gb300.amplifier): one 3 m ARK4IP solve per
     precision on its cluster class, timed with CUDA events, with the df and mixed outputs'
@@ -546,6 +583,8 @@ def run_ours(a):
             acc["vs"] = "fp64 engine plan on the same inputs, every member"
         if "mixed" in leg_out and a.precision != "mixed":
             legs["mixed"]["accuracy_vs_fp64"] = accuracy(leg_out["mixed"])
+            legs["mixed"]["replay_of_fp64_steps"] = replay_experiment(
+                a, members, domains, fields, leg_out, local)
         legs["fp64"]["accuracy"] = ("the reference precision (tests/test_gpu_parity.py and "
                                     "tests/test_gpu_ensemble_parity.py: <= 1e-9 against the FP64 oracle)")
 

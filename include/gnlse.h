@@ -240,6 +240,22 @@ int gnlse_set_class_cost(int precision, int log2_points_per_cta, int cluster, do
  * in normal builds.  Synchronises the device. */
 int gnlse_profile_counters(gnlse_plan* plan, long long* out);
 
+/* Record the accepted steps of adaptive instance `instance` on the following propagate
+ * calls: entry k of d_steps (device, 2 * capacity doubles) is (z, h) of accepted step k,
+ * the z reached and the step size used, as Stepper.adaptive_stepper appends them to
+ * Storage.step_sizes (pyofss/modules/stepper.py:339-345; pyofss keeps only the steps
+ * that store a trace, the log keeps every one).  gnlse_stats.steps counts them; steps
+ * beyond `capacity` are not recorded.  capacity 0 stops the log.  Synchronous. */
+int gnlse_set_step_log(gnlse_plan* plan, int instance, double* d_steps, int64_t capacity);
+
+/* Replay: ARK4IP instance `instance` takes its step sizes from d_h (device, n doubles,
+ * e.g. a step log) and accepts every attempt, ending after n steps; the step-doubling
+ * error estimate is still formed (gnlse_stats.delta_last).  The oracle's
+ * adaptive(replay=...) does the same on the CPU.  No counterpart in the reference's
+ * stepper: it separates the effect of arithmetic precision on a propagation from that of
+ * the step-size controller's decisions.  n 0 returns to the controller.  Synchronous. */
+int gnlse_set_replay(gnlse_plan* plan, int instance, const double* d_h, int64_t n);
+
 /* Copy per-instance statistics to host memory (synchronises `stream`). */
 int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
 

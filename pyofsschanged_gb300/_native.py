@@ -97,6 +97,8 @@ SIGNATURES = {
                                    ct.c_int64, ct.c_void_p]),
     "gnlse_propagate_host": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "gnlse_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(Stats), ct.c_void_p]),
+    "gnlse_set_step_log": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int64]),
+    "gnlse_set_replay": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int64]),
     "gnlse_set_timing": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "gnlse_profile_counters": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_longlong)]),
     "gnlse_propagate_noalloc": (ct.c_int, [ct.POINTER(GridDesc), ct.POINTER(InstanceDesc),

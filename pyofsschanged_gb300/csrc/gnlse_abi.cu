@@ -828,6 +828,27 @@ int gnlse_class_order(gnlse_plan* p, int32_t* order) {
   return GNLSE_OK;
 }
 
+int gnlse_set_step_log(gnlse_plan* p, int instance, double* d_steps, int64_t capacity) {
+  if (!p || instance < 0 || instance >= (int)p->inst.size() || capacity < 0 || (capacity > 0 && !d_steps))
+    return GNLSE_BAD_ARGUMENT;
+  InstDev& d = p->inst[instance];
+  d.step_log = capacity > 0 ? d_steps : nullptr;
+  d.step_cap = capacity;
+  cudaError_t e = cudaMemcpy(p->d_inst + instance, &d, sizeof(InstDev), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? GNLSE_OK : cuda_fail(e);
+}
+
+int gnlse_set_replay(gnlse_plan* p, int instance, const double* d_h, int64_t n) {
+  if (!p || instance < 0 || instance >= (int)p->inst.size() || n < 0 || (n > 0 && !d_h))
+    return GNLSE_BAD_ARGUMENT;
+  InstDev& d = p->inst[instance];
+  if (n > 0 && d.method != GNLSE_ARK4IP) return GNLSE_UNSUPPORTED;
+  d.replay = n > 0 ? d_h : nullptr;
+  d.replay_n = n;
+  cudaError_t e = cudaMemcpy(p->d_inst + instance, &d, sizeof(InstDev), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? GNLSE_OK : cuda_fail(e);
+}
+
 int gnlse_get_stats(gnlse_plan* p, gnlse_stats* out, void* stream) {
   if (!p || !out) return GNLSE_BAD_ARGUMENT;
   const size_t n = p->inst.size();

@@ -1679,6 +1679,10 @@ struct Engine {
         const bool accept = delta < 2.0 * d.tol;
         __syncthreads();
         if (threadIdx.x == 0) {
+          if (accept && d.step_log && st.steps < d.step_cap && cx.rank == 0) {
+            d.step_log[2 * st.steps] = st.z + h;
+            d.step_log[2 * st.steps + 1] = h;
+          }
           st.evals += 3;
           st.attempts += 1;
           st.ta += 1;
@@ -1722,7 +1726,14 @@ struct Engine {
       // ---- one attempt (adaptive) or one step (fixed) ------------------------
       if (threadIdx.x == 0) {
         if (adaptive) {
-          if (st.ta == 0) {
+          if (d.replay) {  // follow the given step sizes; the list ends the propagation
+            if (st.steps >= d.replay_n) {
+              st.status = ST_OK;
+              st.phase = 2;
+            } else {
+              st.h = d.replay[st.steps];
+            }
+          } else if (st.ta == 0) {
             if (st.steps >= 99999) {  // for s in range(1, steps_max) (stepper.py:289)
               st.status = ST_MAX_STEPS;
               st.phase = 2;
@@ -1858,9 +1869,13 @@ struct Engine {
         const double nf = sqrt(nrm[1]);
         delta = nf != 0.0 ? sqrt(nrm[0]) / nf : sqrt(nrm[0]);
       }
-      const bool accept = delta < 2.0 * d.tol;
+      const bool accept = d.replay != nullptr || delta < 2.0 * d.tol;
       __syncthreads();
       if (threadIdx.x == 0) {
+        if (accept && d.step_log && st.steps < d.step_cap && cx.rank == 0) {
+          d.step_log[2 * st.steps] = st.z + h;
+          d.step_log[2 * st.steps + 1] = h;
+        }
         st.attempts += 1;
         st.ta += 1;
         st.delta_last = delta;

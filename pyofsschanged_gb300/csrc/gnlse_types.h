@@ -52,6 +52,10 @@ struct InstDev {
   long long scratch_off;// element offset of the 8*N scratch block
   long long trace_off;  // element offset of max_traces*N trace slots
   long long tracez_off; // index of this instance's first trace z value
+  double* step_log;     // adaptive: accepted steps (z, h), 2 doubles each (null: none)
+  const double* replay; // adaptive RK4IP: step sizes to follow, every attempt accepted (null: none)
+  long long step_cap;   // capacity of step_log in steps
+  long long replay_n;   // entries of replay
 };
 
 enum : int {

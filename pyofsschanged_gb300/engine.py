@@ -208,6 +208,38 @@ class Plan:
             k += cnt
         return out
 
+    def set_step_log(self, i, capacity):
+        """Record instance i's accepted steps (z, h) from the next propagate on
+        (gnlse_set_step_log); capacity 0 stops.  step_log(i) reads them."""
+        if not hasattr(self, "_step_logs"):
+            self._step_logs = {}
+        buf = torch.zeros(2 * max(int(capacity), 1), dtype=torch.float64, device=self.device)
+        self._step_logs[i] = buf if capacity > 0 else None
+        nat.check(nat.lib().gnlse_set_step_log(self.handle, int(i), ct.c_void_p(buf.data_ptr()),
+                                               int(capacity)), "gnlse_set_step_log")
+
+    def step_log(self, i, stats=None):
+        """[(z, h)] of instance i's recorded accepted steps (numpy, k x 2)."""
+        buf = getattr(self, "_step_logs", {}).get(i)
+        if buf is None:
+            return np.zeros((0, 2))
+        k = min((stats or self.stats())[i]["steps"], buf.numel() // 2)
+        return buf[:2 * k].view(k, 2).cpu().numpy()
+
+    def set_replay(self, i, h):
+        """Make ARK4IP instance i follow the step sizes h (every attempt accepted);
+        None returns it to the step-size controller (gnlse_set_replay)."""
+        if not hasattr(self, "_replays"):
+            self._replays = {}
+        if h is None:
+            self._replays.pop(i, None)
+            nat.check(nat.lib().gnlse_set_replay(self.handle, int(i), ct.c_void_p(), 0), "gnlse_set_replay")
+            return
+        t = torch.as_tensor(np.asarray(h, float), dtype=torch.float64).to(self.device).contiguous()
+        self._replays[i] = t
+        nat.check(nat.lib().gnlse_set_replay(self.handle, int(i), ct.c_void_p(t.data_ptr()), t.numel()),
+                  "gnlse_set_replay")
+
     def stats(self, stream=None):
         s = stream or torch.cuda.current_stream(self.device)
         arr = (nat.Stats * len(self.instances))()

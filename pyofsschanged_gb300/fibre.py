@@ -87,6 +87,18 @@ def raise_for_status(status):
         raise nat.GnlseError(status, "propagation")
 
 
+def trace_steps(log, length, traces):
+    """The accepted steps (z, h) the adaptive stepper keeps in Storage.step_sizes: those
+    with z > z_ignore, z_ignore advancing by length / traces (stepper.py:339-345)."""
+    out, step = [], length / traces
+    z_ignore = step
+    for z, h in log:
+        if z > z_ignore:
+            out.append((float(z), float(h)))
+            z_ignore += step
+    return out
+
+
 CHARACT_LISTS = ("energy_list", "max_power_list", "peaks_list", "duration_list", "spec_width_list",
                  "l_nl_list", "l_d_list")
 
@@ -203,6 +215,8 @@ class Fibre:
         inst = Instance(0, method=st.method, length=self.length, local_error=st.local_error,
                         total_steps=st.total_steps, traces=st.traces)
         self._plan = Plan([g], [inst], precision=self.precision)
+        if st.adaptive:  # every accepted step, up to the stepper's steps_max (stepper.py:130)
+            self._plan.set_step_log(0, 100000)
         self.domain = domain
         st.storage(domain)
 
@@ -216,6 +230,11 @@ class Fibre:
         torch.cuda.current_stream(plan.device).synchronize()
         z, As = plan.instance_traces(0, stats, device=True)
         return plan.unpack(flat)[0].cpu().numpy().astype(complex), stats[0], z, As
+
+    def _step_sizes(self, st):
+        """Storage.step_sizes (stepper.py:339-345): (z, h) of the accepted steps that stored
+        a trace, from the engine's log of every accepted step."""
+        return trace_steps(self._plan.step_log(0, [st]), self.length, self.stepper.traces)
 
     def __call__(self, domain, field):
         if self.domain != domain or self._plan is None:
@@ -234,8 +253,7 @@ class Fibre:
             ch = trace_characteristics(As, domain, self.gamma, beta2)
             for k in CHARACT_LISTS:
                 setattr(storage, k, ch[k])
-        if self.stepper.adaptive:
-            storage.step_sizes = []
+        storage.step_sizes = self._step_sizes(st) if self.stepper.adaptive else []
         storage.fft_total = int(st["evals"]) * 16
         raise_for_status(st["status"])
         return out

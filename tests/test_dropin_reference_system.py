@@ -49,7 +49,11 @@ class OracleEngineFibre(cf.Fibre):
         out, info = p.adaptive(np.array(field, complex), st.local_error, st.total_steps, st.traces)
         stats = {"status": self.status, "evals": p.evals, "pump_w": 0.0}
         tr = np.array(info["trace_A"]).reshape(-1, grid.total_samples)
+        self._oracle_steps = info["steps"]
         return out, stats, np.array(info["trace_z"]), torch.as_tensor(tr)
+
+    def _step_sizes(self, st):
+        return cf.trace_steps(self._oracle_steps, self.length, self.stepper.traces)
 
 
 def _reference_system(case, fibre):
@@ -87,6 +91,8 @@ def test_cuda_fibre_runs_in_reference_system():
     assert sys_.df_results is None
     storage = fib.stepper.storage
     np.testing.assert_allclose(storage.z, case["trace_z"], rtol=1e-14, atol=0)
+    # Storage.step_sizes by the reference's rule (z > z_ignore) from the log of every step
+    np.testing.assert_allclose(np.array(storage.step_sizes), case["step_sizes"], rtol=1e-13, atol=0)
     assert len(storage.As) == len(storage.energy_list) == len(case["trace_z"])
 
 
