@@ -207,6 +207,11 @@ struct Engine {
   static constexpr int NR16 = LOGM / RB;        // passes of the main radix
   static constexpr int REM = LOGM % RB;         // log2 of the final smaller radix
   static constexpr int RED = 64;  // doubles of reduction scratch
+  // cluster_sum keeps up to 3 partial sums per warp at red[0, 48) and the totals at
+  // red[48, 51): CTAs of at most 16 warps (a 1024-thread CTA would write past red into
+  // the control block)
+  static_assert(3 * (((M / PPT) < GNLSE_TMIN ? GNLSE_TMIN : (M / PPT)) / 32) <= 48,
+                "reduction scratch holds the partial sums of at most 16 warps");
   static_assert(LOGM >= 8, "M >= 256 required");
   static_assert(C == 1 || C == 2 || C == 4 || C == 8 || C == 16, "cluster size 1, 2, 4, 8 or 16");
   static constexpr size_t ctl_bytes() { return 1024; }
