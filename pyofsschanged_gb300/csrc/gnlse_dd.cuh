@@ -91,4 +91,58 @@ __device__ __forceinline__ ddc cmulc(ddc a, ddc b) {  // a * conj(b)
   return ddc{dd_dot2(a.x, b.x, a.y, b.y), dd_dot2(a.y, b.x, -a.x, b.y)};
 }
 
+#ifndef GNLSE_DF_LAZY
+#define GNLSE_DF_LAZY 1
+#endif
+#if GNLSE_DF_LAZY
+// Lazy variants for the inside of a DFT butterfly: the same error-free transformations
+// without the final renormalisation, so the low word may exceed half an ulp of the high
+// word; a two-sum of the high words stays exact for any inputs and the low words only
+// accumulate, so a few lazy operations in a row keep the double-word accuracy.  The
+// butterfly renormalises its outputs once (cnorm) before they are stored.
+__device__ __forceinline__ ddf dd_add_lazy(ddf a, ddf b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ddf(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ddf dd_dot2_lazy(ddf a, ddf b, ddf c, ddf d) {  // a b + c d
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float q = __fmul_rn(c.hi, d.hi);
+  const float ep = fmaf(a.hi, b.hi, -p);
+  const float eq = fmaf(c.hi, d.hi, -q);
+  const float s = __fadd_rn(p, q);
+  const float bb = __fsub_rn(s, p);
+  const float t = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(q, bb));
+  float lo = __fadd_rn(__fadd_rn(t, ep), eq);
+  lo = fmaf(a.hi, b.lo, lo);
+  lo = fmaf(a.lo, b.hi, lo);
+  lo = fmaf(c.hi, d.lo, lo);
+  lo = fmaf(c.lo, d.hi, lo);
+  return ddf(s, lo);
+}
+__device__ __forceinline__ ddc cadd_lazy(ddc a, ddc b) { return ddc{dd_add_lazy(a.x, b.x), dd_add_lazy(a.y, b.y)}; }
+__device__ __forceinline__ ddc csub_lazy(ddc a, ddc b) { return ddc{dd_add_lazy(a.x, -b.x), dd_add_lazy(a.y, -b.y)}; }
+__device__ __forceinline__ ddc cmul_lazy(ddc a, ddc b) {
+  return ddc{dd_dot2_lazy(a.x, b.x, -a.y, b.y), dd_dot2_lazy(a.x, b.y, a.y, b.x)};
+}
+__device__ __forceinline__ ddc cmulc_lazy(ddc a, ddc b) {
+  return ddc{dd_dot2_lazy(a.x, b.x, a.y, b.y), dd_dot2_lazy(a.y, b.x, -a.x, b.y)};
+}
+// renormalisation after lazy operations: a full two-sum, since cancellation of the high
+// words may leave the low word the larger
+__device__ __forceinline__ ddf dd_norm(ddf a) {
+  const float s = __fadd_rn(a.hi, a.lo);
+  const float bb = __fsub_rn(s, a.hi);
+  return ddf(s, __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(a.lo, bb)));
+}
+#if GNLSE_DF_LAZY == 2
+// trial: no renormalisation at the butterfly outputs either (the next operation that is
+// not lazy renormalises)
+__device__ __forceinline__ ddc cnorm(ddc a) { return a; }
+#else
+__device__ __forceinline__ ddc cnorm(ddc a) { return ddc{dd_norm(a.x), dd_norm(a.y)}; }
+#endif
+#endif
+
 }  // namespace gnlse

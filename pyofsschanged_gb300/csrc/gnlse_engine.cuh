@@ -94,6 +94,13 @@ template <class V> __device__ __forceinline__ V cmulc(V a, V b) {  // a * conj(b
   return mk<V>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 template <class V, class S> __device__ __forceinline__ V cscale(V a, S s) { return mk<V>(a.x * s, a.y * s); }
+// inside a DFT butterfly: the plain operations, or for double-float values the variants
+// that skip the renormalisation (gnlse_dd.cuh), with one cnorm of each output
+template <class V> __device__ __forceinline__ V cadd_lazy(V a, V b) { return cadd(a, b); }
+template <class V> __device__ __forceinline__ V csub_lazy(V a, V b) { return csub(a, b); }
+template <class V> __device__ __forceinline__ V cmul_lazy(V a, V b) { return cmul(a, b); }
+template <class V> __device__ __forceinline__ V cmulc_lazy(V a, V b) { return cmulc(a, b); }
+template <class V> __device__ __forceinline__ V cnorm(V a) { return a; }
 template <class V> __device__ __forceinline__ auto cabs2(V a) -> decltype(a.x) { return a.x * a.x + a.y * a.y; }
 
 // Padded shared-memory slot: one spare element every 16 makes every Stockham
@@ -152,8 +159,8 @@ __device__ __forceinline__ void dft(V (&v)[RAD]) {
 #pragma unroll
       for (int j = 0; j < half; ++j) {
         V a = v[blk + j], b = v[blk + j + half];
-        v[blk + j] = cadd(a, b);
-        V d = csub(a, b);
+        v[blk + j] = cadd_lazy(a, b);
+        V d = csub_lazy(a, b);
         const int m = j * (16 / L);
         if (m == 0) {
           v[blk + j + half] = d;
@@ -161,7 +168,7 @@ __device__ __forceinline__ void dft(V (&v)[RAD]) {
           v[blk + j + half] = SIGN > 0 ? mk<V>(-d.y, d.x) : mk<V>(d.y, -d.x);
         } else {
           const S c = (S)c16(m), s = (S)(SIGN * s16(m));
-          v[blk + j + half] = cmul(d, mk<V>(c, s));  // d.x c - d.y s + i (d.x s + d.y c)
+          v[blk + j + half] = cmul_lazy(d, mk<V>(c, s));  // d.x c - d.y s + i (d.x s + d.y c)
         }
       }
     }
@@ -170,7 +177,7 @@ __device__ __forceinline__ void dft(V (&v)[RAD]) {
 #pragma unroll
   for (int k = 0; k < RAD; ++k) t[k] = v[bitrev(k, B)];
 #pragma unroll
-  for (int k = 0; k < RAD; ++k) v[k] = t[k];
+  for (int k = 0; k < RAD; ++k) v[k] = cnorm(t[k]);
 }
 
 // Simpson weight (units of dt) of sample n out of N, reproducing scipy's
@@ -340,7 +347,8 @@ struct Engine {
           V w[RAD];
           load_row<RAD>(cx.twp + OFF + k * RAD, w);
 #pragma unroll
-          for (int r = 1; r < RAD; ++r) v[b][r] = SIGN > 0 ? cmul(v[b][r], w[r]) : cmulc(v[b][r], w[r]);
+          for (int r = 1; r < RAD; ++r)
+            v[b][r] = SIGN > 0 ? cmul_lazy(v[b][r], w[r]) : cmulc_lazy(v[b][r], w[r]);
         }
         dft<RAD, SIGN>(v[b]);
         const int base = (j - k) * RAD + k;

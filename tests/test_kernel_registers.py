@@ -20,10 +20,11 @@ pytestmark = pytest.mark.skipif(shutil.which("nvcc") is None, reason="no nvcc")
 
 # (unit, most registers, most spill-store bytes of the RK4IP-loop kernel entry).  With
 # the exponential split steps in a kernel of their own and the Yb inversion sums inlined,
-# ptxas reports 312 bytes for the 8 x 2048 mixed class (744 with both loops in one
-# kernel) and none for the one-CTA mixed class and the df classes of the benchmark.
+# ptxas reports 232-312 bytes for the 8 x 2048 mixed class (744 with both loops in one
+# kernel), none for the one-CTA classes and 140 for the 8 x 2048 df class (whose lazy
+# butterflies are 3-5% faster than renormalising ones despite them).
 BUDGET = [("gnlse_inst_mix_m11_c8.cu", 128, 400), ("gnlse_inst_mix_m12_c1.cu", 128, 64),
-          ("gnlse_inst_df_m11_c8.cu", 128, 64), ("gnlse_inst_df_m12_c1.cu", 128, 64)]
+          ("gnlse_inst_df_m11_c8.cu", 128, 200), ("gnlse_inst_df_m12_c1.cu", 128, 64)]
 
 
 @pytest.mark.parametrize("unit,max_regs,max_spill", BUDGET)
