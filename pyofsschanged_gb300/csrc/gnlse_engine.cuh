@@ -476,7 +476,7 @@ struct Engine {
         if (PM % T == 0 || q < PM) {
           const int n2 = cx.rank * PM + q;
 #pragma unroll
-          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul_lazy(v[b][k1], twid(cx.tw, n2 * k1, -1));
           dft<C, -1>(v[b]);
 #pragma unroll
           for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
@@ -509,7 +509,7 @@ struct Engine {
       if (PM % T == 0 || q < PM) {
         const int n2 = cx.rank * PM + q;
 #pragma unroll
-        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], w[b][k1]);
+        for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul_lazy(v[b][k1], w[b][k1]);
         dft<C, -1>(v[b]);
 #pragma unroll
         for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
@@ -569,7 +569,7 @@ struct Engine {
 #pragma unroll
           for (int k1 = 0; k1 < C; ++k1) v[b][k1] = cx.P[pad(tslot(k1, n2))];
 #pragma unroll
-          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul(v[b][k1], twid(cx.tw, n2 * k1, -1));
+          for (int k1 = 1; k1 < C; ++k1) v[b][k1] = cmul_lazy(v[b][k1], twid(cx.tw, n2 * k1, -1));
           dft<C, -1>(v[b]);
 #pragma unroll
           for (int n1 = 0; n1 < C; ++n1) epi(n1, n2, v[b][n1]);
