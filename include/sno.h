@@ -16,7 +16,8 @@ extern "C" {
 
 enum { SNO_OK = 0, SNO_BAD_ARGUMENT = 4, SNO_CUDA_ERROR = 5 };
 
-/* Batched GEMM on BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation):
+/* Batched GEMM on the BF16 tensor cores (tcgen05.mma, kind::f16, FP32 accumulator in
+ * tensor memory; 128 x 64 output tiles, 64-deep K tiles staged in shared memory):
  *   C[z] = alpha * op(A[z]) * op(B[z]) + beta * C[z] (+ bias[n]),  z < batch,
  * op(A) = A (M x K, A[m*lda + k]) or, with ta = 1, A^T stored K x M (A[k*lda + m]);
  * op(B) = B (K x N, B[k*ldb + n]) or, with tb = 1, B^T stored N x K (B[n*ldb + k]).
@@ -28,6 +29,10 @@ int sno_gemm(int M, int N, int K, int ta, int tb, const void* A, long long lda, 
              long long ldb, long long sB, float* C, long long ldc, long long sC, int batch, float alpha,
              float beta, const float* bias, void* gelu_out, void* bf16_out, long long sO, int splits,
              void* stream);
+
+/* Number of GEMM CTAs (since the library was loaded) whose wait for the tensor cores
+ * ran out of its iteration bound; they skipped the rest of their tile.  Synchronous. */
+int sno_gemm_timeouts(unsigned* out);
 
 /* dz = dy * GELU'(zpre) (tanh form), optionally also as BF16 into dz_bf16. */
 int sno_gelu_backward(const float* dy, const float* zpre, float* dz, void* dz_bf16, long long n, void* stream);

@@ -120,6 +120,7 @@ SIGNATURES = {
     "sno_gelu_backward": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                      ct.c_longlong, ct.c_void_p]),
     "sno_to_bf16": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_longlong, ct.c_void_p]),
+    "sno_gemm_timeouts": (ct.c_int, [ct.POINTER(ct.c_uint)]),
     "sno_colsum": (ct.c_int, [ct.c_void_p, ct.c_longlong, ct.c_int, ct.c_void_p, ct.c_void_p]),
     "sno_adam": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                             ct.c_longlong, ct.c_float, ct.c_float, ct.c_float, ct.c_float,
@@ -128,7 +129,7 @@ SIGNATURES = {
                               ct.c_void_p, ct.c_void_p]),
 }
 
-OPTIONAL = {"gnlse_propagate_noalloc", "sno_gemm", "sno_gelu_backward", "sno_to_bf16", "sno_colsum",
+OPTIONAL = {"gnlse_propagate_noalloc", "sno_gemm", "sno_gemm_timeouts", "sno_gelu_backward", "sno_to_bf16", "sno_colsum",
             "sno_adam", "sno_rel_l2"}
 
 _lib = None

@@ -12,7 +12,6 @@
 
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 32, KP = BK + 8;  // padded k stride (bank-conflict free)
 
 __device__ __forceinline__ float gelu_f(float z) {
   // tanh form of GELU (Hendrycks & Gimpel)
@@ -27,18 +26,60 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * du;
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+// ---- tcgen05 GEMM -----------------------------------------------------------
+// One CTA of 128 threads computes a 128 x 64 tile of C with the 5th-generation tensor
+// cores: BF16 tiles of op(A) (128 x 64) and op(B)^T (64 x 64) are staged in shared
+// memory in the canonical K-major layout without swizzle (8 x 8 "core matrices" of
+// 128 contiguous bytes), one thread issues tcgen05.mma (kind::f16, FP32 accumulator in
+// tensor memory, M = 128, N = 64, K = 16 per instruction) and commits to an mbarrier;
+// after the last K tile each warp reads its 32 accumulator lanes (rows) with
+// tcgen05.ld and applies the epilogue.  Every wait is bounded: on a timeout the kernel
+// records it (sno_gemm_timeouts) and skips the rest of its work.
+constexpr int TM = 128, TN = 64, TK = 64, KG = TK / 8;  // KG: 8-element K groups per tile row
+constexpr int TMEM_COLS = 64;                             // FP32 accumulator columns (N)
+constexpr unsigned long long WAIT_LIMIT = 1ull << 26;
+
+__device__ unsigned int g_gemm_timeouts;
+
+// byte offset of element (row, k) of a tile in the canonical K-major layout
+__device__ __forceinline__ int core_off(int row, int k) {
+  return ((row >> 3) * KG + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// shared-memory matrix descriptor: start address, leading byte offset (between core
+// matrices adjacent in K), stride byte offset (between 8-row groups), version 1,
+// no swizzle
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
+  const unsigned long long lbo = 128, sbo = KG * 128;
+  return (unsigned long long)((addr >> 4) & 0x3FFF) | (((lbo >> 4) & 0x3FFF) << 16) |
+         (((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, N = 64, M = 128
+constexpr unsigned IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(TN >> 3) << 17) |
+                           ((unsigned)(TM >> 4) << 24);
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned phase) {
+  for (unsigned long long it = 0; it < WAIT_LIMIT; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
 }
 
 // C[z] (M x N, row-major, ldc) = alpha * op(A[z]) op(B[z]) + beta * C[z] (+ bias[n]);
 // op(A) is M x K: A[m*lda + k] (ta = 0) or A[k*lda + m] (ta = 1);
 // op(B) is K x N: B[k*ldb + n] (tb = 0) or B[n*ldb + k] (tb = 1).
-// Grid: (ceil(N/BN), ceil(M/BM), batch * splits).  With splits > 1 each CTA sums
+// Grid: (ceil(N/TN), ceil(M/TM), batch * splits).  With splits > 1 each CTA sums
 // a K range and adds alpha * partial into C atomically (C prepared by the caller).
 // Epilogue (splits == 1): Z = result is stored to C; if gelu_out, GELU(Z) is
 // also stored as BF16 to gelu_out (same ldc); if bf16_out, Z as BF16.
@@ -59,94 +100,136 @@ struct GemmArgs {
 };
 
 __global__ void __launch_bounds__(128) sno_gemm_kernel(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 As[BM][KP];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN][KP];
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* As = sm;                      // TM x TK BF16, canonical layout (16 KB)
+  unsigned char* Bs = sm + TM * TK * 2;        // TN x TK BF16 (8 KB)
+  unsigned long long* bar = (unsigned long long*)(Bs + TN * TK * 2);
+  unsigned* tmem_slot = (unsigned*)(bar + 1);
   const int z = blockIdx.z / g.splits, sp = blockIdx.z % g.splits;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
   const __nv_bfloat16* A = g.A + (long long)z * g.sA;
   const __nv_bfloat16* B = g.B + (long long)z * g.sB;
   float* C = g.C + (long long)z * g.sC;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  const int gq = lane >> 2, tq = lane & 3;
-  // K range of this split, in BK chunks
-  const int nk = (g.K + BK - 1) / BK;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nk = (g.K + TK - 1) / TK;
   const int per = (nk + g.splits - 1) / g.splits;
   const int kb0 = sp * per, kb1 = min(nk, kb0 + per);
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  const unsigned bar_a = smem_u32(bar);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {  // tensor-memory accumulator: 128 lanes x 64 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int kb = kb0; kb < kb1; ++kb) {
-    const int k0 = kb * BK;
-    // global -> shared: BM x BK of op(A) and BN x BK of op(B)^T, k contiguous in shared
-    for (int e = tid; e < BM * BK; e += 128) {
+  unsigned phase = 0;
+  bool ok = true;
+  for (int kb = kb0; kb < kb1 && ok; ++kb) {
+    const int k0 = kb * TK;
+    // global -> shared in the canonical layout: op(A) rows m, op(B)^T rows n, k inner
+    for (int e = tid; e < TM * TK; e += 128) {
       int m, k;
-      if (g.ta) { m = e % BM; k = e / BM; } else { k = e % BK; m = e / BK; }
+      if (g.ta) { m = e % TM; k = e / TM; } else { k = e % TK; m = e / TK; }
       const int gm = m0 + m, gk = k0 + k;
       __nv_bfloat16 v = zero;
       if (gm < g.M && gk < g.K) v = g.ta ? A[(long long)gk * g.lda + gm] : A[(long long)gm * g.lda + gk];
-      As[m][k] = v;
+      *reinterpret_cast<__nv_bfloat16*>(As + core_off(m, k)) = v;
     }
-    for (int e = tid; e < BN * BK; e += 128) {
+    for (int e = tid; e < TN * TK; e += 128) {
       int n, k;
-      if (g.tb) { k = e % BK; n = e / BK; } else { n = e % BN; k = e / BN; }
+      if (g.tb) { k = e % TK; n = e / TK; } else { n = e % TN; k = e / TN; }
       const int gn = n0 + n, gk = k0 + k;
       __nv_bfloat16 v = zero;
       if (gn < g.N && gk < g.K) v = g.tb ? B[(long long)gn * g.ldb + gk] : B[(long long)gk * g.ldb + gn];
-      Bs[n][k] = v;
+      *reinterpret_cast<__nv_bfloat16*>(Bs + core_off(n, k)) = v;
     }
+    // the generic-proxy stores must be visible to the tensor cores' async proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[2][4], bf[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm + i * 16 + gq;
-        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tq]);
-        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tq]);
-        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tq + 8]);
-        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tq + 8]);
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      for (int j = 0; j < TK / 16; ++j) {
+        const unsigned long long ad = smem_desc(smem_u32(As) + j * 256);
+        const unsigned long long bd = smem_desc(smem_u32(Bs) + j * 256);
+        const unsigned acc = (kb > kb0 || j > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+            : "memory");
       }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = wn + j * 8 + gq;
-        bf[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tq]);
-        bf[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bf[j]);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a)
+                   : "memory");
     }
+    // the MMAs have read the tiles before they are overwritten or the result is read
+    ok = mbar_wait(bar_a, phase);
+    phase ^= 1;
     __syncthreads();
   }
-  // epilogue
+  if (!ok && lane == 0) atomicAdd(&g_gemm_timeouts, 1u);
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+  if (ok && kb1 > kb0) {
+    // this warp's 32 accumulator lanes = rows 32 warp + lane, columns 0..63
+    float acc[TN];
+    {
+      unsigned r[TN];
+      const unsigned taddr = tmem + ((unsigned)(32 * warp) << 16);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+          "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+          "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+            "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+            "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+            "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]),
+            "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]),
+            "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]),
+            "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+            "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int m = m0 + wm + i * 16 + gq + (r >> 1) * 8;
-        const int n = n0 + wn + j * 8 + 2 * tq + (r & 1);
-        if (m >= g.M || n >= g.N) continue;
+      for (int c = 0; c < TN; ++c) acc[c] = __uint_as_float(r[c]);
+    }
+    const int m = m0 + 32 * warp + lane;
+    if (m < g.M) {
+#pragma unroll 8
+      for (int c = 0; c < TN; ++c) {
+        const int n = n0 + c;
+        if (n >= g.N) break;
         float* cp = C + (long long)m * g.ldc + n;
-        const float v = g.alpha * acc[i][j][r];
+        const float v = g.alpha * acc[c];
         if (g.splits > 1) {
           atomicAdd(cp, v);
           continue;
         }
-        float zv = v + (g.beta != 0.f ? g.beta * *cp : 0.f) + (g.bias ? g.bias[n] : 0.f);
+        const float zv = v + (g.beta != 0.f ? g.beta * *cp : 0.f) + (g.bias ? g.bias[n] : 0.f);
         *cp = zv;
         const long long o = (long long)z * g.sO + (long long)m * g.ldc + n;
         if (g.gelu_out) g.gelu_out[o] = __float2bfloat16(gelu_f(zv));
         if (g.bf16_out) g.bf16_out[o] = __float2bfloat16(zv);
       }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
 __global__ void gelu_backward_kernel(const float* dy, const float* zpre, float* dz, __nv_bfloat16* dz16,
@@ -230,6 +313,11 @@ int grid1(long long n) {
 
 extern "C" {
 
+int sno_gemm_timeouts(unsigned* out) {
+  if (!out) return SNO_BAD_ARGUMENT;
+  return cudaMemcpyFromSymbol(out, g_gemm_timeouts, sizeof(unsigned)) == cudaSuccess ? SNO_OK : SNO_CUDA_ERROR;
+}
+
 int sno_gemm(int M, int N, int K, int ta, int tb, const void* A, long long lda, long long sA, const void* B,
              long long ldb, long long sB, float* C, long long ldc, long long sC, int batch, float alpha,
              float beta, const float* bias, void* gelu_out, void* bf16_out, long long sO, int splits,
@@ -247,9 +335,14 @@ int sno_gemm(int M, int N, int K, int ta, int tb, const void* A, long long lda, 
   g.batch = batch; g.splits = splits;
   const long long gz = (long long)batch * splits;
   if (gz > 65535) return SNO_BAD_ARGUMENT;
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, (unsigned)gz);
+  dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, (unsigned)gz);
   if (grid.y > 65535) return SNO_BAD_ARGUMENT;
-  sno_gemm_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(g);
+  // 24 KB of tiles plus the barrier; 36 KB requested keeps at most 6 CTAs (384 of the 512
+  // tensor-memory columns) on an SM
+  const int smem = 36 * 1024;
+  if (cudaFuncSetAttribute(sno_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return SNO_CUDA_ERROR;
+  sno_gemm_kernel<<<grid, 128, smem, (cudaStream_t)stream>>>(g);
   return cudaGetLastError() == cudaSuccess ? SNO_OK : SNO_CUDA_ERROR;
 }
 

@@ -49,6 +49,14 @@ def _check(code, what):
         raise RuntimeError(f"{what} failed (status {code})")
 
 
+def gemm_timeouts():
+    """GEMM CTAs whose bounded wait for the tensor cores ran out (0 in a healthy run)."""
+    lib = nat.lib()
+    out = ct.c_uint(0)
+    _check(lib.sno_gemm_timeouts(ct.byref(out)), "sno_gemm_timeouts")
+    return int(out.value)
+
+
 def gemm(M, N, K, A, B, C, ta=0, tb=0, lda=None, ldb=None, ldc=None, sA=0, sB=0, sC=0, batch=1,
          alpha=1.0, beta=0.0, bias=None, gelu_out=None, bf16_out=None, sO=0, splits=1, a_off=0, b_off=0,
          c_off=0, o_off=0, stream=None):

@@ -48,6 +48,7 @@ def test_gemm_matches_torch(cuda_ready, ta, tb):
         sg.gemm(M, N, K, A, B, C2, ta=ta, tb=tb, sA=A[0].numel(), sB=B[0].numel(), sC=M * N, batch=batch,
                 beta=1.0, splits=3)
         assert torch.allclose(C2, torch.bmm(a, b) + C0, rtol=1e-4, atol=1e-4 * K ** 0.5)
+    assert sg.gemm_timeouts() == 0
 
 
 def test_forward_and_gradients_match_oracle(cuda_ready):
