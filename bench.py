@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-attempts", type=int, default=20,
                     help="attempts per grid size timed on the plain single-instance GPU path")
+    ap.add_argument("--surrogate-train", type=int, default=2000,
+                    help="training pulses of the surrogate leg (0: skip it)")
     ap.add_argument("--batched-iterations", type=int, default=12,
                     help="timed iterations per grid and batch size of the batched library "
                          "comparator (0: skip it)")
@@ -620,6 +622,18 @@ def run_ours(a):
     # the iterations the members' attempt counts (this run's) need, grids one after another
     amp = amplifier_leg(local) if (a.legs and rank == 0) else None
 
+    # learned surrogate with RK4IP fallback, on a reduced training set (the full 20k-sample
+    # experiment is python -m pyofsschanged_gb300.surrogate_run): acceptance and solves/s
+    # against the engine on the same held-out pulses
+    sur = None
+    if a.legs and rank == 0 and a.surrogate_train > 0:
+        from pyofsschanged_gb300 import surrogate_run
+        r = surrogate_run.run(["--train", str(a.surrogate_train), "--calib", "200", "--test", "500",
+                               "--epochs", "3"])
+        sur = {"train": a.surrogate_train, "test": 500, "epochs": 3, "train_s": r["train_s"],
+               "test_error": r["test_error"], "engine_solves_per_s": r["engine_solves_per_s_test"],
+               "with_fallback": r["surrogate_with_fallback"]}
+
     batched = None
     if rank == 0 and a.batched_iterations > 0:
         batched = batched_library_leg(a, members, domains, fields, stats, value, dev)
@@ -648,7 +662,7 @@ def run_ours(a):
                        "evals_per_step": evals},
             "roofline": roofline, "cpu_baseline": cpu_line, "e2e": e2e, "clocks": ck,
             "gpu_launches": launches, "accuracy_vs_fp64": acc, "legs": legs, "plain": plain,
-            "batched_library": batched, "amplifier_2e16": amp,
+            "batched_library": batched, "amplifier_2e16": amp, "surrogate": sur,
             "coherence": coherence,
             "class_ms": {f"m2^{lm}_c{c}_n{cnt}": statistics.mean(st[k][3] for st in class_ms)
                          for k, (lm, c, cnt, _) in enumerate(class_ms[0])}}

@@ -36,6 +36,12 @@ def solve_chunked(A0, z, chunk=4096):
 
 
 def main(argv=None):
+    run(argv)
+    return 0
+
+
+def run(argv=None):
+    """The whole experiment; returns the result dictionary (also printed as one JSON line)."""
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--calib", type=int, default=1000)
@@ -116,7 +122,7 @@ def main(argv=None):
     if a.out:
         with open(a.out, "w") as f:
             f.write(line + "\n")
-    return 0
+    return res
 
 
 if __name__ == "__main__":
