@@ -194,6 +194,19 @@ cudaError_t upload(gnlse_plan* p, const std::vector<T>& h, void** d) {
   return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// Complex tables of double-float plans in the engine's layout {re.hi, im.hi, re.lo, im.lo}
+// (gnlse_dd.cuh): each complex entry is built as two ddf (re, im) and rearranged.
+template <class R>
+void pack_complex(std::vector<R>& v) {
+  if constexpr (std::is_same<R, ddf>::value) {
+    for (size_t i = 0; i + 1 < v.size(); i += 2) {
+      const ddf r = v[i], m = v[i + 1];
+      v[i] = ddf(r.hi, m.hi);
+      v[i + 1] = ddf(r.lo, m.lo);
+    }
+  }
+}
+
 // R: the transform element's real type (float, double or the double-float ddf);
 // extended: mixed-precision plans (FP64 boundary twiddles); want_cis: the
 // double-float cis(j pi / 512) table of the exp(hD) factors (mixed and df plans)
@@ -248,6 +261,9 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
     twl[2 * (size_t)j] = tw[2 * (size_t)j * C];
     twl[2 * (size_t)j + 1] = tw[2 * (size_t)j * C + 1];
   }
+  pack_complex(tw);
+  pack_complex(twl);
+  pack_complex(Hp);
   // per-pass twiddle rows of the M-point transform
   const int rb = std::is_same<R, ddf>::value ? GNLSE_DF_RADIX_BITS : GNLSE_RADIX_BITS;  // the engine's radix
   const int logm = gh.logm, ntwp = twp_size(logm, rb);
@@ -264,6 +280,7 @@ cudaError_t build_grid_tables(gnlse_plan* p, const gnlse_grid_desc& gd, GridHost
       twp64[2 * (size_t)e2 + 1] = sn;
     }
   }
+  pack_complex(twp);
   cudaError_t e;
   if ((e = upload(p, twp, &gh.d_twp)) != cudaSuccess) return e;
   if (extended && (e = upload(p, twp64, &gh.d_twp64)) != cudaSuccess) return e;

@@ -78,13 +78,31 @@ __device__ __forceinline__ T ldro(const T* p) {
     return ddf(v.x, v.y);
   } else if constexpr (std::is_same<T, ddc>::value) {
     const float4 v = __ldg(reinterpret_cast<const float4*>(p));
-    return ddc{ddf(v.x, v.y), ddf(v.z, v.w)};
+    return ddc{make_float2(v.x, v.y), make_float2(v.z, v.w)};
   } else {
     return __ldg(p);
   }
 }
 
-template <class V> __device__ __forceinline__ V mk(decltype(V::x) a, decltype(V::x) b) { V r; r.x = a; r.y = b; return r; }
+// real type of a complex element type, its parts and construction
+template <class V> struct RT { using type = decltype(V::x); };
+template <> struct RT<ddc> { using type = ddf; };
+template <class V> __device__ __forceinline__ V mk(typename RT<V>::type a, typename RT<V>::type b) {
+  if constexpr (std::is_same<V, ddc>::value) {
+    return mkdc(a, b);
+  } else {
+    V r;
+    r.x = a;
+    r.y = b;
+    return r;
+  }
+}
+template <class V> __device__ __forceinline__ auto re(const V& a) -> decltype(a.x) { return a.x; }
+template <class V> __device__ __forceinline__ auto im(const V& a) -> decltype(a.y) { return a.y; }
+template <class V> __device__ __forceinline__ V cconj(V a) { return mk<V>(a.x, -a.y); }
+template <int SIGN, class V> __device__ __forceinline__ V cmul_i(V a) {  // SIGN i a
+  return SIGN > 0 ? mk<V>(-a.y, a.x) : mk<V>(a.y, -a.x);
+}
 template <class V> __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
 template <class V> __device__ __forceinline__ V csub(V a, V b) { return mk<V>(a.x - b.x, a.y - b.y); }
 template <class V> __device__ __forceinline__ V cmul(V a, V b) {
@@ -148,7 +166,7 @@ __device__ __forceinline__ constexpr double s16(int m) { return c16(m - 4); }
 // radix-2 decimation in frequency with constant twiddles, output in natural order.
 template <int RAD, int SIGN, class V>
 __device__ __forceinline__ void dft(V (&v)[RAD]) {
-  using S = decltype(V::x);
+  using S = typename RT<V>::type;
   constexpr int B = ilog2(RAD);
 #pragma unroll
   for (int st = 0; st < B; ++st) {
@@ -165,7 +183,7 @@ __device__ __forceinline__ void dft(V (&v)[RAD]) {
         if (m == 0) {
           v[blk + j + half] = d;
         } else if (m == 4) {  // multiply by SIGN*i
-          v[blk + j + half] = SIGN > 0 ? mk<V>(-d.y, d.x) : mk<V>(d.y, -d.x);
+          v[blk + j + half] = cmul_i<SIGN>(d);
         } else {
           const S c = (S)c16(m), s = (S)(SIGN * s16(m));
           v[blk + j + half] = cmul_lazy(d, mk<V>(c, s));  // d.x c - d.y s + i (d.x s + d.y c)
@@ -293,9 +311,8 @@ struct Engine {
   // non-coherent loads may be hoisted across the barriers into earlier
   // passes, which lengthens register lifetimes until the kernel spills.
   static __device__ __forceinline__ V twid(const V* tw, int idx, int sign) {
-    V w = tw[idx];
-    if (sign < 0) w.y = -w.y;
-    return w;
+    const V w = tw[idx];
+    return sign < 0 ? cconj(w) : w;
   }
 
   // ---- transforms ---------------------------------------------------------
@@ -724,7 +741,7 @@ struct Engine {
         const int s = pad(tslot(n1, n2));
         V x = X[s];
         R p = cabs2(x);
-        X[s] = cmul(x, mk<V>(f1 * p + fR * conv.x, fR * conv.y));
+        X[s] = cmul(x, mk<V>(f1 * p + fR * re(conv), fR * im(conv)));
       };
       inv(cx, P, rdPH, e3, false);
     }
@@ -737,7 +754,7 @@ struct Engine {
   // local time slots, sample tsample(rank, slot)), summed over the cluster.
   static __device__ double simpson_energy(const Ctx& cx, const GridDev& g, const V* buf) {
     double e = 0.0;
-    for (int l = threadIdx.x; l < M; l += T) e += simpson_w(tsample(cx.rank, l), N) * (double)buf[pad(l)].x;
+    for (int l = threadIdx.x; l < M; l += T) e += simpson_w(tsample(cx.rank, l), N) * (double)re(buf[pad(l)]);
     double s[1] = {e * g.dt * 1e-3};
     cluster_sum<1>(cx, s);
     return s[0];
@@ -777,14 +794,14 @@ struct Engine {
   // user field element <-> transform element (double-float plans convert complex128)
   static __device__ __forceinline__ V fv2v(const FV& f) {
     if constexpr (DD) {
-      return V{R(f.x), R(f.y)};
+      return mk<V>(R(f.x), R(f.y));
     } else {
       return f;
     }
   }
   static __device__ __forceinline__ FV v2fv(const V& v) {
     if constexpr (DD) {
-      return make_double2((double)v.x, (double)v.y);
+      return make_double2((double)re(v), (double)im(v));
     } else {
       return v;
     }
@@ -863,10 +880,10 @@ struct Engine {
           dfc_store(E1, a, e);
           if (E2) dfc_store(E2, a, dfc_mul(e, e));
         } else {
-          E1[a] = V{ddf(e.re.hi, e.re.lo), ddf(e.im.hi, e.im.lo)};
+          E1[a] = mk<V>(ddf(e.re.hi, e.re.lo), ddf(e.im.hi, e.im.lo));
           if (E2) {
             const dfc e2 = dfc_mul(e, e);
-            E2[a] = V{ddf(e2.re.hi, e2.re.lo), ddf(e2.im.hi, e2.im.lo)};
+            E2[a] = mk<V>(ddf(e2.re.hi, e2.re.lo), ddf(e2.im.hi, e2.im.lo));
           }
         }
       }
@@ -925,7 +942,7 @@ struct Engine {
     for (int l = threadIdx.x; l < M; l += T) {
       const int a = base + l;
       const V v = src == 0 ? op.MA0[a] : (src == 1 ? ldv(op.acc, a) : cx.X[pad(l)]);
-      const double p = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+      const double p = (double)re(v) * (double)re(v) + (double)im(v) * (double)im(v);
       const double2 ww = __ldg(&w[a]);
       s0 += ww.x * p;
       s1 += ww.y * p;
@@ -960,7 +977,7 @@ struct Engine {
       return v;
     }
   }
-  static __device__ __forceinline__ V ik(R k, V v) { return mk<V>(-k * v.y, k * v.x); }  // i k v
+  static __device__ __forceinline__ V ik(R k, V v) { return cscale(cmul_i<1>(v), k); }  // i k v
 
   template <int U, class In, class Ld, class St>
   static __device__ __forceinline__ void each_slot(Ld&& ld, St&& st) {
@@ -1124,7 +1141,7 @@ struct Engine {
       auto rdPH = [&](int o, int l) -> V { return cmul(P[pad(l)], ldro(&Hp[o * M + l])); };
       auto e3 = [&](int n1, int n2, V conv) {
         const int sl = pad(tslot(n1, n2));
-        P[sl] = mk<V>(f1 * cabs2(X[sl]) + fR * conv.x, fR * conv.y);
+        P[sl] = mk<V>(f1 * cabs2(X[sl]) + fR * re(conv), fR * im(conv));
       };
       inv(cx, P, rdPH, e3);
     }
@@ -1134,7 +1151,7 @@ struct Engine {
     for (int l = threadIdx.x; l < M; l += T) {
       const V t = P[pad(l)];
       const V b = Bt[tsample(cx.rank, l)];
-      const R px = (R)(-gh) * t.y, py = (R)gh * t.x;
+      const R px = (R)(-gh) * im(t), py = (R)gh * re(t);
       V ephi;
       if constexpr (DD) {  // the phase factor in FP64, ~1e-16, rounded to double-float
         double sn, cs;
@@ -1242,14 +1259,14 @@ struct Engine {
   // ss_agrawal's ratio n(y)/y where |y| > 1e-5, else 0 (solver.py:295-316), in FP64
   // (out of line: FP64 library code, called from every transform epilogue site)
   static __device__ __noinline__ V agr_ratio(V n, V y) {
-    const double yr = (double)y.x, yi = (double)y.y;
+    const double yr = (double)re(y), yi = (double)im(y);
     if (!(hypot(yr, yi) > 1.0e-5)) return mk<V>(R(0.0), R(0.0));
-    const double nr = (double)n.x, ni = (double)n.y, d = yr * yr + yi * yi;
+    const double nr = (double)re(n), ni = (double)im(n), d = yr * yr + yi * yi;
     return mk<V>(R((nr * yr + ni * yi) / d), R((ni * yr - nr * yi) / d));
   }
   // exp(hh r) - 1 = expm1(x) cos y - 2 sin^2(y/2) + i e^x sin y, x + i y = hh r, in FP64
   static __device__ __noinline__ V cexpm1_scaled(double hh, V r) {
-    const double x = hh * (double)r.x, y = hh * (double)r.y;
+    const double x = hh * (double)re(r), y = hh * (double)im(r);
     double sn, cs;
     sincos(y, &sn, &cs);
     const double hs = sin(0.5 * y), em1 = expm1(x);
@@ -1351,12 +1368,12 @@ struct Engine {
         dfc_store(Cc, a, dfc_add(dfc_scale(f, df_from_double(fa)), dfc_scale(c, df_from_double(-fb))));
       } else {
         const V f = F[a], c = Cc[a];
-        const double fr = (double)f.x, fi = (double)f.y;
-        const double dr = fr - (double)c.x, di = fi - (double)c.y;
+        const double fr = (double)re(f), fi = (double)im(f);
+        const double dr = fr - (double)re(c), di = fi - (double)im(c);
         d2 += dr * dr + di * di;
         f2 += fr * fr + fi * fi;
         if (!isfinite(fr) || !isfinite(fi)) bad = 1.0;
-        Cc[a] = mk<V>(R(fa) * f.x - R(fb) * c.x, R(fa) * f.y - R(fb) * c.y);
+        Cc[a] = mk<V>(R(fa) * re(f) - R(fb) * re(c), R(fa) * im(f) - R(fb) * im(c));
       }
     }
     s[0] = d2;
@@ -1438,8 +1455,8 @@ struct Engine {
               const V d = csub(sf, res);
               d2 += cabs2(d);
               f2 += cabs2(sf);
-              if (!isfinite(sf.x) || !isfinite(sf.y)) bad = 1.0;
-              op.out[a] = mk<V>(fa * sf.x - fb * res.x, fa * sf.y - fb * res.y);
+              if (!isfinite(re(sf)) || !isfinite(im(sf))) bad = 1.0;
+              op.out[a] = mk<V>(fa * re(sf) - fb * re(res), fa * im(sf) - fb * im(res));
             }
           }
         });
@@ -1544,7 +1561,7 @@ struct Engine {
   static __device__ __forceinline__ bool rk_method(int method) { return method <= 2; }
 
   template <int KIND>
-  static __device__ void run(const KParams& kp) {
+  static __device__ __forceinline__ void run(const KParams& kp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cid = blockIdx.x / C;
     if (cid >= kp.n_order) return;

@@ -21,10 +21,12 @@ pytestmark = pytest.mark.skipif(shutil.which("nvcc") is None, reason="no nvcc")
 # (unit, most registers, most spill-store bytes of the RK4IP-loop kernel entry).  With
 # the exponential split steps in a kernel of their own and the Yb inversion sums inlined,
 # ptxas reports 232-312 bytes for the 8 x 2048 mixed class (744 with both loops in one
-# kernel), none for the one-CTA classes and 140 for the 8 x 2048 df class (whose lazy
-# butterflies are 3-5% faster than renormalising ones despite them).
+# kernel) and none for its one-CTA classes.  The df classes' paired FP32 instructions
+# need their operands in aligned register pairs: 192 bytes for the 8 x 2048 class (108
+# with scalar instructions) and 84 for the 4096-point one-CTA class (0), which are still
+# 11-13% faster per attempt than the scalar build.
 BUDGET = [("gnlse_inst_mix_m11_c8.cu", 128, 400), ("gnlse_inst_mix_m12_c1.cu", 128, 64),
-          ("gnlse_inst_df_m11_c8.cu", 128, 200), ("gnlse_inst_df_m12_c1.cu", 128, 64)]
+          ("gnlse_inst_df_m11_c8.cu", 128, 240), ("gnlse_inst_df_m12_c1.cu", 128, 128)]
 
 
 @pytest.mark.parametrize("unit,max_regs,max_spill", BUDGET)
@@ -35,6 +37,9 @@ def test_hot_class_register_budget(tmp_path, unit, max_regs, max_spill):
          "-c", os.path.join(CSRC, unit), "-o", str(tmp_path / "unit.o")],
         check=True, capture_output=True, text=True).stderr
     lines = out.splitlines()
+    # the propagation loop is inlined into the kernel entry (a call to an out-of-line
+    # copy of it passes its state through the stack and spills around the call)
+    assert not any("Function properties for" in ln and "3runILi" in ln for ln in lines)
     i = next(k for k, ln in enumerate(lines) if "Function properties for _ZN5gnlse12gnlse_kernel" in ln)
     spill = int(re.search(r"(\d+) bytes spill stores", lines[i + 1]).group(1))
     regs = int(re.search(r"Used (\d+) registers", lines[i + 2]).group(1))
