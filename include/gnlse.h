@@ -271,8 +271,8 @@ int gnlse_get_stats(gnlse_plan* plan, gnlse_stats* out, void* stream);
  * in place).  Larger grids and the Yb model return GNLSE_UNSUPPORTED.  All calls share the
  * array: calls whose GPU work overlaps (other streams or threads) race and
  * must be serialised by the caller.  The first call on each device looks up
- * the array's address; make it before any stream capture.  The call waits for
- * its host-to-device table copies; stats_out (optional) waits for the result. */
+ * the array's address.  The call waits for its host-to-device table copies;
+ * stats_out (optional) waits for the result. */
 int gnlse_propagate_noalloc(const gnlse_grid_desc* grid, const gnlse_instance_desc* instance,
                             void* d_field, gnlse_stats* stats_out, void* stream);
 

@@ -152,15 +152,13 @@ __device__ __forceinline__ ddc csub(ddc a, ddc b) {
   return crenorm(l.hi, l.lo);
 }
 // a b (CONJ: a conj(b)) as two double-word dot products, component 0 = a.x b.x -+ a.y b.y
-// and component 1 = a.y b.x +- a.x b.y: the products of a with (b.x, b.x) and of the
-// swapped a = (a.y, a.x) with (-+b.y, +-b.y), their exact rounding errors (FMA) and the
-// cross terms in the low word; low word not renormalised
+// and component 1 = a.y b.x +- a.x b.y: the products of a with bx = (b.x, b.x) and of the
+// swapped a = (a.y, a.x) (negated for CONJ) with ny = (-b.y, b.y), their exact rounding
+// errors (FMA) and the cross terms in the low word; low word not renormalised.
 template <bool CONJ>
-__device__ __forceinline__ ddc cmul_pair(ddc a, ddc b) {
-  const float2 bxh = make_float2(b.hi.x, b.hi.x), bxl = make_float2(b.lo.x, b.lo.x);
-  const float2 nyh = CONJ ? make_float2(b.hi.y, -b.hi.y) : make_float2(-b.hi.y, b.hi.y);
-  const float2 nyl = CONJ ? make_float2(b.lo.y, -b.lo.y) : make_float2(-b.lo.y, b.lo.y);
-  const float2 sh = make_float2(a.hi.y, a.hi.x), sl = make_float2(a.lo.y, a.lo.x);
+__device__ __forceinline__ ddc cmul_bc(ddc a, float2 bxh, float2 nyh, float2 bxl, float2 nyl) {
+  const float2 sh = CONJ ? make_float2(-a.hi.y, -a.hi.x) : make_float2(a.hi.y, a.hi.x);
+  const float2 sl = CONJ ? make_float2(-a.lo.y, -a.lo.x) : make_float2(a.lo.y, a.lo.x);
   const float2 p = f2mul(a.hi, bxh);
   const float2 q = f2mul(sh, nyh);
   const float2 ep = f2fma(a.hi, bxh, f2neg(p));
@@ -174,6 +172,11 @@ __device__ __forceinline__ ddc cmul_pair(ddc a, ddc b) {
   lo = f2fma(sh, nyl, lo);
   lo = f2fma(sl, nyh, lo);
   return ddc{s, lo};
+}
+template <bool CONJ>
+__device__ __forceinline__ ddc cmul_pair(ddc a, ddc b) {
+  return cmul_bc<CONJ>(a, make_float2(b.hi.x, b.hi.x), make_float2(-b.hi.y, b.hi.y),
+                       make_float2(b.lo.x, b.lo.x), make_float2(-b.lo.y, b.lo.y));
 }
 __device__ __forceinline__ ddc cmul(ddc a, ddc b) {
   const ddc l = cmul_pair<false>(a, b);

@@ -16,8 +16,7 @@
 // overlaps on the GPU (different streams, or different host threads) race
 // and must be serialised by the caller; one call on one stream is ordered.
 // The first call on a device looks up the array's device address (once per
-// device, with that device current); make that first call before any stream
-// capture begins.
+// device, with that device current).
 #include <cuda_runtime.h>
 
 #include <cmath>
