@@ -45,7 +45,7 @@ ENSEMBLE_SEED = 20261203  # sc_ensemble's default seed: rank 0 is the reference 
 # one ncu capture of the class launch on a saturated GPU (608 members x 4 attempts of the
 # 2^14 grid, profiles/gnlse_kernel_df_m11_c8_saturated.md); scales the dominant
 # launch's traffic by its attempts
-DRAM_BYTES_PER_ATTEMPT = {("df", 11, 8): (0.469401856e9 + 2.938670e9) / 2432}
+DRAM_BYTES_PER_ATTEMPT = {("df", 11, 8): (0.715539456e9 + 3.931759e9) / 2432}
 
 
 def parse():
