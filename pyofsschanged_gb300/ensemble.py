@@ -173,11 +173,15 @@ def common_spectra(fields, sizes_min=4096):
 
     With a common dt every grid's frequency points contain those of the
     coarsest grid (every n/n_min-th point), so members are compared bin by bin.
+    Each spectrum is taken with its time origin t = 0 at index 0 (the field
+    rotated by n/2 samples): the grids' windows [-W/2, W/2) differ, and with the
+    window's start as origin the spectra of the same pulse on two grids would
+    differ by a phase exp(i w dW/2), a sign (-1)^k at the odd common bins.
     """
     out = []
     for a in fields:
         n = len(a)
-        spec = fft(np.asarray(a, complex))
+        spec = fft(np.roll(np.asarray(a, complex), -(n // 2)))
         step = n // sizes_min
         out.append(spec[::step] * step)
     return np.array(out)
